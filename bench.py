@@ -1,0 +1,391 @@
+"""Benchmark: particle-steps/s of the PBF step at 1,048,576 particles, 4 iterations.
+
+Workload (the reference's 1M configuration): seeded 128x128x64 dam-break
+lattice, spacing 0.5h, box 12.8x6.4x6.4, h = 0.1, rho0 = 6378, dt = 1/60,
+1 substep, 4 solver iterations, s_corr k = 0.1 n = 4 dq = 0.2h, eps = 600,
+XSPH 0.01, vorticity 1e-4, gravity -9.8.  One step = one step() call.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+value     K steps replayed from HBM-resident state, CUDA events on the
+          launching stream, synchronize on both sides; N ranks = N
+          independent replicas (one process per GPU, no collective on the
+          data path), value = all ranks' particle-steps / max rank time.
+e2e       the same metric through the public API with host buffers: every step
+          uploads positions+velocities from pinned host memory
+          (pbf_set_particles), steps, and downloads positions+velocities to
+          pinned host memory.
+roofline  dominant kernel of the step, timed live with CUDA events captured
+          in the frame graph, against the measured HBM copy bandwidth.
+--impl reference  the CPU restatement of the reference step (the reference
+          has no CPU implementation) on all host cores, bounded sample.
+"""
+
+from __future__ import annotations
+
+import argparse
+import importlib
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s at 1M (4 iters)"
+UNIT = "particle-steps/s"
+WORKLOAD = ("dam_break_1m: 1,048,576 particles (128x128x64 lattice, spacing 0.5h, jitter "
+            "+-0.01h seed 0) in a 12.8x6.4x6.4 box, h=0.1, rho0=6378, dt=1/60, 1 substep, "
+            "4 iterations, scorr k=0.1 n=4 dq=0.2h, eps=600, xsph 0.01, vorticity 1e-4")
+# Algorithmic bytes per particle-step: 492 + I*(128 + 8C) + 8C with I = 4
+# iterations and C = cells/particle (minimal compulsory traffic: integrate,
+# hash, counting sort, reorder, lambda, delta-p + apply, final rebuild, the
+# one-time gather and the four velocity stages).
+def b_alg(iters: int, cells_per_particle: float) -> float:
+    return 492.0 + iters * (128.0 + 8.0 * cells_per_particle) + 8.0 * cells_per_particle
+
+
+# Algorithmic bytes per particle of each stage (same accounting; neighbour
+# data staged on chip, lists counted as zero).
+STAGE_BYTES = {
+    "predict": 64.0 + 20.0,          # R x, v; W x*, v_in; + hash of the first rebuild
+    "sort": 8.0,                      # R key, W permutation
+    "gather": 44.0,                   # R perm, R/W x*, R/W composed permutation
+    "search_lambda": 24.0,            # R x*, W lambda, W count
+    "delta_apply_collide": 56.0,      # R x*, R lambda, W x* + next hash
+    "search_final": 20.0,
+    "finalize": 68.0,
+    "xsph": 48.0,
+    "vorticity": 48.0,
+    "confine_resolve": 64.0,
+}
+
+
+def load_pkg():
+    name = "fluid_simulator_gb300"
+    if name in sys.modules:
+        return sys.modules[name]
+    pkg_dir = os.path.join(ROOT, "fluid-simulator_gb300")
+    spec = importlib.util.spec_from_file_location(name, os.path.join(pkg_dir, "__init__.py"),
+                                                  submodule_search_locations=[pkg_dir])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class Clocks:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join("/tmp", "pbf_clocks_%d_%d.csv" % (os.getpid(), gpu_index))
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        try:
+            os.remove(self.path)
+        except OSError:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        smax = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4)
+                          if r[5 + k].lower().startswith("active")})
+        load = [v for v in sm if smax and v > 0.5 * max(smax)] or sm
+        return {"sm_mhz": statistics.median(load) if load else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def setup_dist(world, local):
+    if world <= 1:
+        return None
+    import torch
+    import torch.distributed as dist
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allreduce_max(dist, v: float) -> float:
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cuda_sync():
+    try:
+        import torch
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
+    except ImportError:
+        pass
+
+
+def pinned_like(a: np.ndarray):
+    """A pinned host copy of `a` (torch pin_memory), as a numpy view."""
+    try:
+        import torch
+        t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        return t, t.numpy()
+    except Exception:
+        return None, np.ascontiguousarray(a).copy()
+
+
+def cpu_baseline(scene, seconds_budget: float = 20.0, threads: int = 0):
+    """FP32 restatement of the reference step (oracle, OpenMP) on the host cores."""
+    from oracle import oracle as O
+    pos, vel, mn, mx, prm, _ = scene
+    threads = threads or os.cpu_count() or 1
+    o = O.OracleSolver(32, threads=threads)
+    o.initialize(len(pos), mn, mx, prm.as_dict())
+    o.set_particles(pos, vel)
+    t0 = time.perf_counter()
+    st = o.step()  # warm-up step (first touch of the lists)
+    warm = time.perf_counter() - t0
+    if st != 0:
+        raise RuntimeError("oracle step failed: %d" % st)
+    steps = max(1, int(seconds_budget / max(warm, 1e-3)))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        st = o.step()
+        if st != 0:
+            raise RuntimeError("oracle step failed: %d" % st)
+    dt = time.perf_counter() - t0
+    return {"value": len(pos) * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": "%d steps of the full %d-particle workload after 1 warm-up step "
+                      "(FP32 C++/OpenMP restatement, %.1f s)" % (steps, len(pos), dt)}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return 0
+    pkg = load_pkg()
+    scenes = importlib.import_module("fluid_simulator_gb300.scenes")
+    scene = scenes.dam_break_1m()
+    budget = float(os.environ.get("PBF_REF_SECONDS", "60"))
+    cb = cpu_baseline(scene, seconds_budget=budget)
+    n = len(scene[0])
+    steps_done = int(round(cb["value"] * budget / n)) if cb["value"] else 0
+    line = {
+        "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
+        "n_gpus": world, "steps": steps_done, "warmup": 1,
+        "ms_per_step": 1000.0 * n / cb["value"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded 128x128x64 dam-break lattice",
+        "config": {"workload": WORKLOAD, "particles": n, "iterations": 4,
+                   "implementation": "CPU restatement of the reference step (the reference "
+                                     "ships CUDA only); bounded sample"},
+        "cpu_baseline": cb,
+        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    del pkg
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--scene", default="dam_break_1m")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.warmup < 3:
+        args.warmup = 3
+
+    rank, world, local = dist_env()
+    dist = setup_dist(world, local)
+    pkg = load_pkg()
+    scenes = importlib.import_module("fluid_simulator_gb300.scenes")
+    scene = scenes.SCENES[args.scene]()
+    pos, vel, mn, mx, prm, col = scene
+    n = len(pos)
+
+    s = pkg.PBFSolver(local)
+    s.initialize(n, mn, mx, prm)
+    for k, fn in (("spheres", s.set_spheres), ("boxes", s.set_boxes), ("planes", s.set_planes)):
+        if col.get(k):
+            fn(col[k])
+    s.set_particles(pos, vel)
+    s.run(args.warmup)
+    kernels = s.kernels_per_frame()
+
+    # ---- device-timed value -------------------------------------------------
+    cuda_sync()
+    barrier(dist)
+    with Clocks(local) as clk:
+        ms = s.time_frames(args.steps)
+    cuda_sync()
+    barrier(dist)
+    ms_max = allreduce_max(dist, ms)
+    value = n * args.steps * world / (ms_max / 1000.0)
+
+    # ---- dominant kernel, timed live in the frame graph ---------------------
+    prof = {}
+    for _ in range(3):
+        for k, (t, c) in s.profile_frame().items():
+            a = prof.setdefault(k, [0.0, 0])
+            a[0] += t
+            a[1] += c
+    stages = {k: {"ms_per_launch": v[0] / v[1], "launches_per_frame": v[1] / 3.0,
+                  "share": 0.0} for k, v in prof.items()}
+    total = sum(v[0] for v in prof.values())
+    for k, v in prof.items():
+        stages[k]["share"] = v[0] / total if total else 0.0
+    dom = max(stages, key=lambda k: prof[k][0])
+    peaks, peak_kind = measured_peaks()
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    dom_bytes = STAGE_BYTES.get(dom, 0.0) * n
+    achieved = dom_bytes / (stages[dom]["ms_per_launch"] / 1000.0) / 1e9
+    cells = 1
+    for a, b_ in zip(mn, mx):
+        cells *= int(np.ceil((np.float64(np.float32(b_)) - np.float64(np.float32(a))) /
+                             np.float64(np.float32(prm.smoothingRadius))))
+    balg = b_alg(prm.solverIterations, cells / n)
+    step_achieved = balg * n * (args.steps / (ms / 1000.0)) / 1e9
+
+    # ---- end to end through the public API with pinned host buffers ---------
+    keep = []
+
+    def pinned(a):
+        t, view = pinned_like(a)
+        keep.append(t)
+        return view
+
+    in_p, in_v = pinned(pos), pinned(vel)
+    out_p, out_v = pinned(np.zeros_like(pos)), pinned(np.zeros_like(vel))
+    s.set_particles(in_p, in_v)
+    s.step()
+    cuda_sync()
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        s.set_particles(in_p, in_v)
+        s.step()
+        s.copy_positions_to_host(out=out_p)
+        s.copy_velocities_to_host(out=out_v)
+        in_p, out_p = out_p, in_p
+        in_v, out_v = out_v, in_v
+    cuda_sync()
+    e2e_s = allreduce_max(dist, time.perf_counter() - t0)
+    e2e_value = n * args.e2e_steps * world / e2e_s
+
+    density = s.density_error()
+
+    line = None
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded 128x128x64 dam-break lattice (no dataset)",
+            "config": {"workload": WORKLOAD if args.scene == "dam_break_1m" else args.scene,
+                       "particles": n, "iterations": prm.solverIterations,
+                       "substeps": prm.substeps, "parallelism": "replicas" if world > 1 else
+                       "single GPU", "l2": "step working set ~250 MB > 129 MB L2 (no flush)",
+                       "timing": "CUDA events around %d graph-replayed steps on the solver "
+                                 "stream" % args.steps},
+            "clocks": clk.summary(),
+            "e2e": {"value": e2e_value, "unit": UNIT,
+                    "h2d_bytes_per_step": int(2 * 16 * n), "d2h_bytes_per_step": int(2 * 16 * n),
+                    "steps": args.e2e_steps,
+                    "path": "pbf_set_particles(pinned host) + pbf_step + "
+                            "pbf_copy_positions/velocities(pinned host) per step"},
+            "gpu_launches": kernels * args.steps,
+            "kernels_per_step": kernels,
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
+                         "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                         "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": dom_bytes,
+                         "ms_per_launch": stages[dom]["ms_per_launch"]},
+            "step_roofline": {"bytes_per_particle_step": balg, "achieved": step_achieved,
+                              "peak": hbm, "unit": "GB/s", "frac": step_achieved / hbm},
+            "stages": stages,
+            "density_error": {"mean": density[0], "max": density[1]},
+        }
+        if not args.no_cpu_baseline and world == 1:
+            budget = float(os.environ.get("PBF_CPU_SECONDS", "20"))
+            line["cpu_baseline"] = cpu_baseline(scene, seconds_budget=budget)
+        print(json.dumps(line), flush=True)
+    s.close()
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

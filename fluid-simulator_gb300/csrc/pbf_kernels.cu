@@ -1,0 +1,547 @@
+// pbf_kernels.cu -- per-particle kernels of the PBF step for sm_103a.
+//
+// Hot path per constraint iteration (reference: src/pbf/pbf_solver.cu:210-258):
+//   k_predict        integrate + v_in copy + first cell keys      (integration.cu:6-32)
+//   [sort]           stable radix sort of (key, index)            (spatial_grid.cu:188-196)
+//   k_cell_ranges    half-open [start, end) per occupied cell     (spatial_grid.cu:123-137)
+//   k_gather_xs      reorder predicted positions + compose the permutation
+//   k_search<true>   neighbour walk + lambda in one pass           (neighbors.cu:3-91,
+//                                                                  pbf_solver_kernels.cu:26-105)
+//   k_delta_apply    delta p + apply + collision projection + next keys
+//                                                                 (pbf_solver_kernels.cu:108-193,
+//                                                                  collision_system.cu:133-172)
+// After the last iteration (pbf_solver.cu:260-323):
+//   k_search<false>  rebuilt lists for the velocity terms
+//   k_finalize       gather x, v_in, ids by the composite permutation + velocity update
+//   k_xsph, k_vorticity, k_confine   (pbf_solver_kernels.cu:213-385), collision
+//                    velocity response fused into the last of them
+//
+// Every floating-point operation uses the explicit-rounding helpers of
+// pbf_math.cuh so the host oracle reproduces the step bit for bit.
+#include "pbf_kernels.cuh"
+
+#include <math_constants.h>
+
+namespace pbf {
+
+namespace {
+
+__device__ __forceinline__ bool fatal(const unsigned* status) {
+    return status != nullptr && (__ldcg(status) & kStatusFatalMask) != 0u;
+}
+
+// ---------------------------------------------------------------------------
+// integrate + collision input velocity + keys of the first rebuild
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kBlock)
+k_predict(const float4* __restrict__ x, const float4* __restrict__ v, float4* __restrict__ xs,
+          float4* __restrict__ vin, uint32_t* __restrict__ keys, int n, StepConst c,
+          const unsigned* __restrict__ status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || fatal(status)) return;
+    float4 vv = v[i];
+    const float4 p = x[i];
+    vv.x = ffma(c.gravx, c.dt, vv.x);
+    vv.y = ffma(c.gravy, c.dt, vv.y);
+    vv.z = ffma(c.gravz, c.dt, vv.z);
+    float4 q;
+    q.x = ffma(vv.x, c.dt, p.x);
+    q.y = ffma(vv.y, c.dt, p.y);
+    q.z = ffma(vv.z, c.dt, p.z);
+    q.w = p.w;
+    xs[i] = q;
+    vin[i] = vv;
+    keys[i] = key_of(c.g, q);
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_cell_ranges(const uint32_t* __restrict__ skeys, int* __restrict__ cs, int* __restrict__ ce,
+              int n, const unsigned* __restrict__ status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || fatal(status)) return;
+    const uint32_t key = skeys[i];
+    if (i == 0 || skeys[i - 1] != key) cs[key] = i;
+    if (i == n - 1 || skeys[i + 1] != key) ce[key] = i + 1;
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_gather_xs(const uint32_t* __restrict__ perm, const float4* __restrict__ xs_in,
+            float4* __restrict__ xs_out, const uint32_t* __restrict__ org_in,
+            uint32_t* __restrict__ org_out, int n, const unsigned* __restrict__ status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || fatal(status)) return;
+    const uint32_t p = perm[i];
+    xs_out[i] = xs_in[p];
+    org_out[i] = org_in ? org_in[p] : p;
+}
+
+// ---------------------------------------------------------------------------
+// Neighbour walk.  Order of the list = z -> y -> x over the clamped cells,
+// ascending sorted index inside a cell, self skipped, accept d2 <= h2
+// (src/pbf/neighbors.cu:319-358).  With LAMBDA the constraint terms of
+// computeLambda are accumulated in that same list order.
+// ---------------------------------------------------------------------------
+struct LambdaAcc {
+    float wsum, s2, gx, gy, gz;
+};
+
+__device__ __forceinline__ void lambda_add(const KernelConst& k, LambdaAcc& a, float dx, float dy,
+                                           float dz, float d2) {
+    a.wsum = fadd(a.wsum, poly6(k, d2));
+    float gx, gy, gz;
+    spiky(k, dx, dy, dz, d2, gx, gy, gz);
+    a.s2 = ffma(gz, gz, ffma(gy, gy, ffma(gx, gx, a.s2)));
+    a.gx = fadd(a.gx, gx);
+    a.gy = fadd(a.gy, gy);
+    a.gz = fadd(a.gz, gz);
+}
+
+__device__ __forceinline__ float lambda_finish(const StepConst& c, const LambdaAcc& a) {
+    const float rho = fmul(c.mass, a.wsum);
+    const float g2 = dist2(a.gx, a.gy, a.gz);
+    const float denom = ffma(c.gs2, fadd(a.s2, g2), c.lambda_eps);
+    const float C = fsub(fdiv(rho, c.rho0), 1.0f);
+    return fdiv(-C, denom);
+}
+
+template <bool LAMBDA>
+__global__ void __launch_bounds__(kBlock)
+k_search(const float4* __restrict__ xs, const int* __restrict__ cs, const int* __restrict__ ce,
+         StepConst c, int n, uint32_t* __restrict__ nbr, int* __restrict__ cnt,
+         float* __restrict__ lam, unsigned* __restrict__ status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || fatal(status)) return;
+    const float4 pi = xs[i];
+    int cx, cy, cz;
+    cell_of(c.g, pi.x, pi.y, pi.z, cx, cy, cz);
+    const int R = c.g.radius;
+    const int x0 = max(0, cx - R), x1 = min(c.g.gx - 1, cx + R);
+    const int y0 = max(0, cy - R), y1 = min(c.g.gy - 1, cy + R);
+    const int z0 = max(0, cz - R), z1 = min(c.g.gz - 1, cz + R);
+    const float h2 = c.k.h2;
+    LambdaAcc acc{c.k.c_poly6, 0.0f, 0.0f, 0.0f, 0.0f};
+    int count = 0;
+    for (int z = z0; z <= z1; ++z) {
+        for (int y = y0; y <= y1; ++y) {
+            for (int x = x0; x <= x1; ++x) {
+                const uint32_t key = cell_key(c.g, x, y, z);
+                const int s = __ldg(&cs[key]);
+                if (s == -1) continue;
+                const int e = __ldg(&ce[key]);
+                for (int j = s; j < e; ++j) {
+                    if (j == i) continue;
+                    const float4 pj = __ldg(&xs[j]);
+                    const float dx = fsub(pi.x, pj.x);
+                    const float dy = fsub(pi.y, pj.y);
+                    const float dz = fsub(pi.z, pj.z);
+                    const float d2 = dist2(dx, dy, dz);
+                    if (d2 <= h2) {
+                        if (count < c.max_nb)
+                            nbr[static_cast<size_t>(count) * c.stride + i] =
+                                static_cast<uint32_t>(j);
+                        ++count;
+                        if (LAMBDA) lambda_add(c.k, acc, dx, dy, dz, d2);
+                    }
+                }
+            }
+        }
+    }
+    cnt[i] = count;
+    if (count > c.max_nb) atomicOr(status, kStatusNeighborOverflow);
+    if (LAMBDA) lam[i] = count > c.max_nb ? CUDART_NAN_F : lambda_finish(c, acc);
+}
+
+__device__ __forceinline__ bool count_ok(int count, int max_nb) {
+    return count >= 0 && count <= max_nb;
+}
+
+// computeDeltaPosition summed in list order (pbf_solver_kernels.cu:134-171).
+__device__ __forceinline__ void delta_sum(const StepConst& c, const float4* __restrict__ xs,
+                                          const uint32_t* __restrict__ nbr,
+                                          const float* __restrict__ lam, int i, int count,
+                                          float4 pi, float& dpx, float& dpy, float& dpz) {
+    const float li = lam[i];
+    float ax = 0.0f, ay = 0.0f, az = 0.0f;
+    for (int k = 0; k < count; ++k) {
+        const uint32_t j = __ldg(&nbr[static_cast<size_t>(k) * c.stride + i]);
+        const float4 pj = __ldg(&xs[j]);
+        const float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y), dz = fsub(pi.z, pj.z);
+        const float d2 = dist2(dx, dy, dz);
+        float gx, gy, gz;
+        spiky(c.k, dx, dy, dz, d2, gx, gy, gz);
+        const float ls = fadd(fadd(li, __ldg(&lam[j])), scorr(c.sc, d2));
+        ax = ffma(ls, gx, ax);
+        ay = ffma(ls, gy, ay);
+        az = ffma(ls, gz, az);
+    }
+    dpx = fmul(c.gs, ax);
+    dpy = fmul(c.gs, ay);
+    dpz = fmul(c.gs, az);
+}
+
+// delta p + applyDeltaPosition + CollisionSystem::solve + next cell keys.
+__global__ void __launch_bounds__(kBlock)
+k_delta_apply(const float4* __restrict__ xs, const uint32_t* __restrict__ nbr,
+              const int* __restrict__ cnt, const float* __restrict__ lam, StepConst c, int n,
+              float4* __restrict__ xs_out, uint32_t* __restrict__ keys_out,
+              unsigned* __restrict__ status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || fatal(status)) return;
+    const float4 pi = xs[i];
+    const int count = cnt[i];
+    float dpx, dpy, dpz;
+    if (!count_ok(count, c.max_nb)) {
+        dpx = dpy = dpz = CUDART_NAN_F;
+    } else {
+        delta_sum(c, xs, nbr, lam, i, count, pi, dpx, dpy, dpz);
+    }
+    float px = fadd(pi.x, dpx), py = fadd(pi.y, dpy), pz = fadd(pi.z, dpz);
+    if (!project_all(c.col, c.particle_radius, px, py, pz))
+        atomicOr(status, kStatusNotConverged);
+    const float4 q = make_float4(px, py, pz, pi.w);
+    xs_out[i] = q;
+    if (keys_out) keys_out[i] = key_of(c.g, q);
+}
+
+// Gather x, v_in, v.w and ids through the composite permutation of the
+// substep, then updateVelocityAndPosition (pbf_solver_kernels.cu:195-211).
+// The new positions are the predicted ones, so xs becomes x without a copy.
+__global__ void __launch_bounds__(kBlock)
+k_finalize(const uint32_t* __restrict__ org, const float4* __restrict__ x_old,
+           const float4* __restrict__ vin_old, const float4* __restrict__ v_old,
+           const uint32_t* __restrict__ id_old, const float4* __restrict__ xs, int n,
+           StepConst c, float4* __restrict__ v_new, float4* __restrict__ vin_new,
+           uint32_t* __restrict__ id_new, const unsigned* __restrict__ status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || fatal(status)) return;
+    const uint32_t o = org[i];
+    const float4 xo = x_old[o];
+    const float4 q = xs[i];
+    float4 vv;
+    vv.x = fmul(fsub(q.x, xo.x), c.inv_dt);
+    vv.y = fmul(fsub(q.y, xo.y), c.inv_dt);
+    vv.z = fmul(fsub(q.z, xo.z), c.inv_dt);
+    vv.w = v_old[o].w;
+    v_new[i] = vv;
+    vin_new[i] = vin_old[o];
+    id_new[i] = id_old[o];
+}
+
+// applyXsphViscosity (pbf_solver_kernels.cu:213-266).
+__device__ __forceinline__ float4 xsph_one(const StepConst& c, const float4* __restrict__ x,
+                                           const float4* __restrict__ v,
+                                           const uint32_t* __restrict__ nbr, int count, int i) {
+    const float4 vi = v[i];
+    if (!count_ok(count, c.max_nb))
+        return make_float4(CUDART_NAN_F, CUDART_NAN_F, CUDART_NAN_F, vi.w);
+    const float4 pi = x[i];
+    float cx = 0.0f, cy = 0.0f, cz = 0.0f;
+    for (int k = 0; k < count; ++k) {
+        const uint32_t j = __ldg(&nbr[static_cast<size_t>(k) * c.stride + i]);
+        const float4 pj = __ldg(&x[j]);
+        const float4 vj = __ldg(&v[j]);
+        const float w = poly6(c.k, dist2(fsub(pi.x, pj.x), fsub(pi.y, pj.y), fsub(pi.z, pj.z)));
+        cx = ffma(fsub(vj.x, vi.x), w, cx);
+        cy = ffma(fsub(vj.y, vi.y), w, cy);
+        cz = ffma(fsub(vj.z, vi.z), w, cz);
+    }
+    return make_float4(ffma(c.xsph_c, cx, vi.x), ffma(c.xsph_c, cy, vi.y),
+                       ffma(c.xsph_c, cz, vi.z), vi.w);
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_xsph(const float4* __restrict__ x, const float4* __restrict__ v,
+       const uint32_t* __restrict__ nbr, const int* __restrict__ cnt, StepConst c, int n,
+       float4* __restrict__ v_out, const float4* __restrict__ vin, bool resolve,
+       const unsigned* __restrict__ status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || fatal(status)) return;
+    float4 out = xsph_one(c, x, v, nbr, cnt[i], i);
+    if (resolve)
+        resolve_velocity(c.col, c.particle_radius, c.restitution, c.friction, x[i], vin[i], out);
+    v_out[i] = out;
+}
+
+// computeVorticity (pbf_solver_kernels.cu:268-315).
+__global__ void __launch_bounds__(kBlock)
+k_vorticity(const float4* __restrict__ x, const float4* __restrict__ v,
+            const uint32_t* __restrict__ nbr, const int* __restrict__ cnt, StepConst c, int n,
+            float4* __restrict__ omega, const unsigned* __restrict__ status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || fatal(status)) return;
+    const int count = cnt[i];
+    if (!count_ok(count, c.max_nb)) {
+        omega[i] = make_float4(CUDART_NAN_F, CUDART_NAN_F, CUDART_NAN_F, 0.0f);
+        return;
+    }
+    const float4 pi = x[i], vi = v[i];
+    float ox = 0.0f, oy = 0.0f, oz = 0.0f;
+    for (int k = 0; k < count; ++k) {
+        const uint32_t j = __ldg(&nbr[static_cast<size_t>(k) * c.stride + i]);
+        const float4 pj = __ldg(&x[j]);
+        const float4 vj = __ldg(&v[j]);
+        const float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y), dz = fsub(pi.z, pj.z);
+        float gx, gy, gz;
+        spiky(c.k, dx, dy, dz, dist2(dx, dy, dz), gx, gy, gz);
+        const float vx = fsub(vj.x, vi.x), vy = fsub(vj.y, vi.y), vz = fsub(vj.z, vi.z);
+        ox = fadd(ox, crossc(gy, gz, vy, vz));
+        oy = fadd(oy, crossc(gz, gx, vz, vx));
+        oz = fadd(oz, crossc(gx, gy, vx, vy));
+    }
+    omega[i] = make_float4(ox, oy, oz, 0.0f);
+}
+
+// applyVorticityConfinement (pbf_solver_kernels.cu:317-385).
+__device__ __forceinline__ float4 confine_one(const StepConst& c, const float4* __restrict__ x,
+                                              const uint32_t* __restrict__ nbr, int count,
+                                              const float4* __restrict__ om,
+                                              const float4* __restrict__ v, int i) {
+    const float4 vi = v[i];
+    if (!count_ok(count, c.max_nb))
+        return make_float4(CUDART_NAN_F, CUDART_NAN_F, CUDART_NAN_F, vi.w);
+    const float4 pi = x[i], wi = om[i];
+    const float wil = len3(wi.x, wi.y, wi.z);
+    float ex = 0.0f, ey = 0.0f, ez = 0.0f;
+    for (int k = 0; k < count; ++k) {
+        const uint32_t j = __ldg(&nbr[static_cast<size_t>(k) * c.stride + i]);
+        const float4 pj = __ldg(&x[j]);
+        const float4 wj = __ldg(&om[j]);
+        const float wjl = len3(wj.x, wj.y, wj.z);
+        const float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y), dz = fsub(pi.z, pj.z);
+        float gx, gy, gz;
+        spiky(c.k, dx, dy, dz, dist2(dx, dy, dz), gx, gy, gz);
+        const float md = fsub(wjl, wil);
+        ex = ffma(md, gx, ex);
+        ey = ffma(md, gy, ey);
+        ez = ffma(md, gz, ez);
+    }
+    const float el = len3(ex, ey, ez);
+    float nx = 0.0f, ny = 0.0f, nz = 0.0f;
+    if (el > kEtaEpsilon) {
+        nx = fdiv(ex, el);
+        ny = fdiv(ey, el);
+        nz = fdiv(ez, el);
+    }
+    const float cx = fmul(c.vort_eps, crossc(ny, nz, wi.y, wi.z));
+    const float cy = fmul(c.vort_eps, crossc(nz, nx, wi.z, wi.x));
+    const float cz = fmul(c.vort_eps, crossc(nx, ny, wi.x, wi.y));
+    return make_float4(ffma(c.dt, cx, vi.x), ffma(c.dt, cy, vi.y), ffma(c.dt, cz, vi.z), vi.w);
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_confine(const float4* __restrict__ x, const uint32_t* __restrict__ nbr,
+          const int* __restrict__ cnt, const float4* __restrict__ om,
+          const float4* __restrict__ v, StepConst c, int n, float4* __restrict__ v_out,
+          const float4* __restrict__ vin, bool resolve, const unsigned* __restrict__ status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || fatal(status)) return;
+    float4 out = confine_one(c, x, nbr, cnt[i], om, v, i);
+    if (resolve)
+        resolve_velocity(c.col, c.particle_radius, c.restitution, c.friction, x[i], vin[i], out);
+    v_out[i] = out;
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_resolve(const float4* __restrict__ x, const float4* __restrict__ vin, float4* __restrict__ v,
+          StepConst c, int n, const unsigned* __restrict__ status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || fatal(status)) return;
+    float4 vv = v[i];
+    resolve_velocity(c.col, c.particle_radius, c.restitution, c.friction, x[i], vin[i], vv);
+    v[i] = vv;
+}
+
+// scatterFloat4ByStableId (pbf_solver_kernels.cu:418-427).
+__global__ void __launch_bounds__(kBlock)
+k_scatter_by_id(const float4* __restrict__ vals, const uint32_t* __restrict__ id,
+                float4* __restrict__ out, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[id[i]] = vals[i];
+}
+
+__global__ void __launch_bounds__(kBlock) k_iota(uint32_t* a, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) a[i] = static_cast<uint32_t>(i);
+}
+
+// |rho/rho0 - 1| per particle over the current lists.
+__global__ void __launch_bounds__(kBlock)
+k_density(const float4* __restrict__ x, const uint32_t* __restrict__ nbr,
+          const int* __restrict__ cnt, StepConst c, int n, float* __restrict__ err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 pi = x[i];
+    const int count = min(cnt[i], c.max_nb);
+    float wsum = c.k.c_poly6;
+    for (int k = 0; k < count; ++k) {
+        const float4 pj = __ldg(&x[__ldg(&nbr[static_cast<size_t>(k) * c.stride + i])]);
+        wsum = fadd(wsum, poly6(c.k, dist2(fsub(pi.x, pj.x), fsub(pi.y, pj.y), fsub(pi.z, pj.z))));
+    }
+    err[i] = fabsf(fsub(fdiv(fmul(c.mass, wsum), c.rho0), 1.0f));
+}
+
+// --- stage kernels -----------------------------------------------------------
+__global__ void __launch_bounds__(kBlock)
+k_grid_keys(const float4* __restrict__ pos, uint32_t* __restrict__ keys, int n, GridConst g) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) keys[i] = key_of(g, pos[i]);
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_lambda_list(const float4* __restrict__ xs, const uint32_t* __restrict__ nbr,
+              const int* __restrict__ cnt, StepConst c, int n, float* __restrict__ lam) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int count = cnt[i];
+    if (!count_ok(count, c.max_nb)) {
+        lam[i] = CUDART_NAN_F;
+        return;
+    }
+    const float4 pi = xs[i];
+    LambdaAcc acc{c.k.c_poly6, 0.0f, 0.0f, 0.0f, 0.0f};
+    for (int k = 0; k < count; ++k) {
+        const float4 pj = xs[nbr[static_cast<size_t>(k) * c.stride + i]];
+        const float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y), dz = fsub(pi.z, pj.z);
+        lambda_add(c.k, acc, dx, dy, dz, dist2(dx, dy, dz));
+    }
+    lam[i] = lambda_finish(c, acc);
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_delta_list(const float4* __restrict__ xs, const uint32_t* __restrict__ nbr,
+             const int* __restrict__ cnt, const float* __restrict__ lam, StepConst c, int n,
+             float4* __restrict__ delta) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int count = cnt[i];
+    if (!count_ok(count, c.max_nb)) {
+        delta[i] = make_float4(CUDART_NAN_F, CUDART_NAN_F, CUDART_NAN_F, 0.0f);
+        return;
+    }
+    float dx, dy, dz;
+    delta_sum(c, xs, nbr, lam, i, count, xs[i], dx, dy, dz);
+    delta[i] = make_float4(dx, dy, dz, 0.0f);
+}
+
+// kind: 0 container, 1 spheres, 2 boxes, 3 planes (one pass), 4 converge all.
+__global__ void __launch_bounds__(kBlock)
+k_collide(float4* __restrict__ pos, int n, StepConst c, int kind, unsigned* __restrict__ flag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 p = pos[i];
+    bool mark = false;
+    switch (kind) {
+        case 0: mark = project_container(c.col, c.particle_radius, p.x, p.y, p.z); break;
+        case 1: mark = project_spheres(c.col, c.particle_radius, p.x, p.y, p.z); break;
+        case 2: mark = project_boxes(c.col, c.particle_radius, p.x, p.y, p.z); break;
+        case 3: mark = project_planes(c.col, c.particle_radius, p.x, p.y, p.z); break;
+        default: mark = !project_all(c.col, c.particle_radius, p.x, p.y, p.z); break;
+    }
+    if (mark) atomicOr(flag, 1u);
+    pos[i] = p;
+}
+
+__global__ void __launch_bounds__(kBlock)
+k_integrate(const float4* __restrict__ x, float4* __restrict__ xs, float4* __restrict__ v,
+            int n, StepConst c) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 vv = v[i];
+    const float4 p = x[i];
+    vv.x = ffma(c.gravx, c.dt, vv.x);
+    vv.y = ffma(c.gravy, c.dt, vv.y);
+    vv.z = ffma(c.gravz, c.dt, vv.z);
+    v[i] = vv;
+    xs[i] = make_float4(ffma(vv.x, c.dt, p.x), ffma(vv.y, c.dt, p.y), ffma(vv.z, c.dt, p.z), p.w);
+}
+
+}  // namespace
+
+// --- launchers ---------------------------------------------------------------
+void launch_predict(const float4* x, const float4* v, float4* xs, float4* vin, uint32_t* keys,
+                    int n, const StepConst& c, const unsigned* status, cudaStream_t st) {
+    k_predict<<<blocks_for(n), kBlock, 0, st>>>(x, v, xs, vin, keys, n, c, status);
+}
+void launch_cell_ranges(const uint32_t* skeys, int* cs, int* ce, int n, const unsigned* status,
+                        cudaStream_t st) {
+    k_cell_ranges<<<blocks_for(n), kBlock, 0, st>>>(skeys, cs, ce, n, status);
+}
+void launch_gather_xs(const uint32_t* perm, const float4* xs_in, float4* xs_out,
+                      const uint32_t* org_in, uint32_t* org_out, int n, const unsigned* status,
+                      cudaStream_t st) {
+    k_gather_xs<<<blocks_for(n), kBlock, 0, st>>>(perm, xs_in, xs_out, org_in, org_out, n, status);
+}
+void launch_search(const float4* xs, const int* cs, const int* ce, const StepConst& c, int n,
+                   uint32_t* nbr, int* cnt, float* lam, unsigned* status, bool with_lambda,
+                   cudaStream_t st) {
+    if (with_lambda)
+        k_search<true><<<blocks_for(n), kBlock, 0, st>>>(xs, cs, ce, c, n, nbr, cnt, lam, status);
+    else
+        k_search<false><<<blocks_for(n), kBlock, 0, st>>>(xs, cs, ce, c, n, nbr, cnt, lam, status);
+}
+void launch_delta_apply(const float4* xs, const uint32_t* nbr, const int* cnt, const float* lam,
+                        const StepConst& c, int n, float4* xs_out, uint32_t* keys_out,
+                        unsigned* status, cudaStream_t st) {
+    k_delta_apply<<<blocks_for(n), kBlock, 0, st>>>(xs, nbr, cnt, lam, c, n, xs_out, keys_out,
+                                                    status);
+}
+void launch_finalize(const uint32_t* org, const float4* x_old, const float4* vin_old,
+                     const float4* v_old, const uint32_t* id_old, const float4* xs, int n,
+                     const StepConst& c, float4* v_new, float4* vin_new, uint32_t* id_new,
+                     const unsigned* status, cudaStream_t st) {
+    k_finalize<<<blocks_for(n), kBlock, 0, st>>>(org, x_old, vin_old, v_old, id_old, xs, n, c,
+                                                 v_new, vin_new, id_new, status);
+}
+void launch_xsph(const float4* x, const float4* v, const uint32_t* nbr, const int* cnt,
+                 const StepConst& c, int n, float4* v_out, const float4* vin, bool resolve,
+                 const unsigned* status, cudaStream_t st) {
+    k_xsph<<<blocks_for(n), kBlock, 0, st>>>(x, v, nbr, cnt, c, n, v_out, vin, resolve, status);
+}
+void launch_vorticity(const float4* x, const float4* v, const uint32_t* nbr, const int* cnt,
+                      const StepConst& c, int n, float4* omega, const unsigned* status,
+                      cudaStream_t st) {
+    k_vorticity<<<blocks_for(n), kBlock, 0, st>>>(x, v, nbr, cnt, c, n, omega, status);
+}
+void launch_confine(const float4* x, const uint32_t* nbr, const int* cnt, const float4* omega,
+                    const float4* v, const StepConst& c, int n, float4* v_out,
+                    const float4* vin, bool resolve, const unsigned* status, cudaStream_t st) {
+    k_confine<<<blocks_for(n), kBlock, 0, st>>>(x, nbr, cnt, omega, v, c, n, v_out, vin, resolve,
+                                                status);
+}
+void launch_resolve(const float4* x, const float4* vin, float4* v, const StepConst& c, int n,
+                    const unsigned* status, cudaStream_t st) {
+    k_resolve<<<blocks_for(n), kBlock, 0, st>>>(x, vin, v, c, n, status);
+}
+void launch_scatter_by_id(const float4* vals, const uint32_t* id, float4* out, int n,
+                          cudaStream_t st) {
+    k_scatter_by_id<<<blocks_for(n), kBlock, 0, st>>>(vals, id, out, n);
+}
+void launch_iota(uint32_t* a, int n, cudaStream_t st) {
+    k_iota<<<blocks_for(n), kBlock, 0, st>>>(a, n);
+}
+void launch_density(const float4* x, const uint32_t* nbr, const int* cnt, const StepConst& c,
+                    int n, float* err, cudaStream_t st) {
+    k_density<<<blocks_for(n), kBlock, 0, st>>>(x, nbr, cnt, c, n, err);
+}
+void launch_grid_keys(const float4* pos, uint32_t* keys, int n, const GridConst& g,
+                      cudaStream_t st) {
+    k_grid_keys<<<blocks_for(n), kBlock, 0, st>>>(pos, keys, n, g);
+}
+void launch_lambda_list(const float4* xs, const uint32_t* nbr, const int* cnt,
+                        const StepConst& c, int n, float* lam, cudaStream_t st) {
+    k_lambda_list<<<blocks_for(n), kBlock, 0, st>>>(xs, nbr, cnt, c, n, lam);
+}
+void launch_delta_list(const float4* xs, const uint32_t* nbr, const int* cnt, const float* lam,
+                       const StepConst& c, int n, float4* delta, cudaStream_t st) {
+    k_delta_list<<<blocks_for(n), kBlock, 0, st>>>(xs, nbr, cnt, lam, c, n, delta);
+}
+void launch_collide(float4* pos, int n, const StepConst& c, int kind, unsigned* flag,
+                    cudaStream_t st) {
+    k_collide<<<blocks_for(n), kBlock, 0, st>>>(pos, n, c, kind, flag);
+}
+void launch_integrate(const float4* x, float4* xs, float4* v, int n, const StepConst& c,
+                      cudaStream_t st) {
+    k_integrate<<<blocks_for(n), kBlock, 0, st>>>(x, xs, v, n, c);
+}
+
+}  // namespace pbf

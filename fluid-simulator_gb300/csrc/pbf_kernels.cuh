@@ -1,0 +1,100 @@
+// pbf_kernels.cuh -- kernel launchers of the PBF step (host-callable).
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "pbf_collide.cuh"
+#include "pbf_math.cuh"
+
+namespace pbf {
+
+// Everything a step kernel needs, passed by value.
+struct StepConst {
+    KernelConst k;
+    ScorrConst sc;
+    GridConst g;
+    Colliders col;
+    float mass, rho0, lambda_eps, gs, gs2;  // gs = mass / rho0
+    float dt, inv_dt;                        // substep dt and 1/dt (host float divide)
+    float gravx, gravy, gravz;
+    float particle_radius, restitution, friction;
+    float xsph_c, vort_eps;
+    int max_nb;
+    size_t stride;  // slot stride of the neighbour lists
+};
+
+constexpr int kBlock = 256;
+
+inline unsigned blocks_for(size_t n, int block = kBlock) {
+    return static_cast<unsigned>((n + block - 1) / block);
+}
+
+// --- step kernels (pbf_kernels.cu) -----------------------------------------
+void launch_predict(const float4* x, const float4* v, float4* xs, float4* vin, uint32_t* keys,
+                    int n, const StepConst& c, const unsigned* status, cudaStream_t st);
+void launch_cell_ranges(const uint32_t* skeys, int* cell_start, int* cell_end, int n,
+                        const unsigned* status, cudaStream_t st);
+void launch_gather_xs(const uint32_t* perm, const float4* xs_in, float4* xs_out,
+                      const uint32_t* org_in, uint32_t* org_out, int n, const unsigned* status,
+                      cudaStream_t st);
+void launch_search(const float4* xs, const int* cell_start, const int* cell_end,
+                   const StepConst& c, int n, uint32_t* nbr, int* cnt, float* lam,
+                   unsigned* status, bool with_lambda, cudaStream_t st);
+void launch_delta_apply(const float4* xs, const uint32_t* nbr, const int* cnt, const float* lam,
+                        const StepConst& c, int n, float4* xs_out, uint32_t* keys_out,
+                        unsigned* status, cudaStream_t st);
+void launch_finalize(const uint32_t* org, const float4* x_old, const float4* vin_old,
+                     const float4* v_old, const uint32_t* id_old, const float4* xs, int n,
+                     const StepConst& c, float4* v_new, float4* vin_new, uint32_t* id_new,
+                     const unsigned* status, cudaStream_t st);
+void launch_xsph(const float4* x, const float4* v, const uint32_t* nbr, const int* cnt,
+                 const StepConst& c, int n, float4* v_out, const float4* vin, bool resolve,
+                 const unsigned* status, cudaStream_t st);
+void launch_vorticity(const float4* x, const float4* v, const uint32_t* nbr, const int* cnt,
+                      const StepConst& c, int n, float4* omega, const unsigned* status,
+                      cudaStream_t st);
+void launch_confine(const float4* x, const uint32_t* nbr, const int* cnt, const float4* omega,
+                    const float4* v, const StepConst& c, int n, float4* v_out,
+                    const float4* vin, bool resolve, const unsigned* status, cudaStream_t st);
+void launch_resolve(const float4* x, const float4* vin, float4* v, const StepConst& c, int n,
+                    const unsigned* status, cudaStream_t st);
+void launch_scatter_by_id(const float4* vals, const uint32_t* id, float4* out, int n,
+                          cudaStream_t st);
+void launch_iota(uint32_t* a, int n, cudaStream_t st);
+void launch_density(const float4* x, const uint32_t* nbr, const int* cnt, const StepConst& c,
+                    int n, float* err, cudaStream_t st);
+
+// --- stage kernels for the standalone entry points -------------------------
+void launch_grid_keys(const float4* pos, uint32_t* keys, int n, const GridConst& g,
+                      cudaStream_t st);
+void launch_lambda_list(const float4* xs, const uint32_t* nbr, const int* cnt,
+                        const StepConst& c, int n, float* lam, cudaStream_t st);
+void launch_delta_list(const float4* xs, const uint32_t* nbr, const int* cnt, const float* lam,
+                       const StepConst& c, int n, float4* delta, cudaStream_t st);
+void launch_collide(float4* pos, int n, const StepConst& c, int kind, unsigned* flag,
+                    cudaStream_t st);
+void launch_integrate(const float4* x, float4* xs, float4* v, int n, const StepConst& c,
+                      cudaStream_t st);
+
+// --- stable LSD radix sort of (key, index) pairs (pbf_sort.cu) ---------------
+struct SortPlan {
+    int n = 0;
+    int tiles = 0;
+    int passes = 0;
+    int bits_per_pass = 0;
+    int bins = 0;
+};
+SortPlan make_sort_plan(int n, uint64_t num_cells);
+// Scratch bytes for hist/totals of a plan with up to n keys.
+size_t sort_scratch_bytes(int max_n);
+// Sorts keys (current order) into sorted_keys/sorted_idx; values start as the
+// identity.  alt_keys/alt_idx are ping-pong buffers of n entries.
+void launch_sort(const SortPlan& plan, const uint32_t* keys, uint32_t* sorted_keys,
+                 uint32_t* sorted_idx, uint32_t* alt_keys, uint32_t* alt_idx, void* scratch,
+                 const unsigned* status, cudaStream_t st);
+// Number of kernel launches launch_sort issues.
+int sort_kernel_count(const SortPlan& plan);
+
+}  // namespace pbf

@@ -1,0 +1,160 @@
+// pbf_math.cuh -- device arithmetic of the PBF step.
+//
+// Every operation is spelled out with a round-to-nearest intrinsic, so the
+// compiler cannot contract or reorder it.  The host oracle performs the same
+// sequence with std::fma and -ffp-contract=off, which makes the whole step
+// bit-reproducible against it.  Formulas restate the reference kernels:
+//   poly6 / spiky gradient  include/pbf/sph_helpers.cuh:13-95
+//   cell hash               include/pbf/spatial_grid.cuh:65-102
+//   artificial pressure     include/pbf/pbf_solver_kernels.cuh:24-47
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace pbf {
+
+constexpr float kPi = 3.14159265358979323846f;
+constexpr int kMaxCollisionPasses = 32;   // src/pbf/collision_system.cu:148
+constexpr float kContactEpsilon = 1e-4f;  // src/pbf/collision_kernels.cu:254
+constexpr float kEtaEpsilon = 1.0e-6f;    // src/pbf/pbf_solver_kernels.cu:367
+constexpr float kProjectionTolScale = 9.5367431640625e-07f;  // 8 * FLT_EPSILON = 2^-20
+
+// Status bits shared by every kernel of a step.  Kernels return early once a
+// fatal bit is set so the state freezes where the reference would throw.
+enum StatusBits : unsigned {
+    kStatusNeighborOverflow = 1u << 0,
+    kStatusNotConverged = 1u << 1,
+    kStatusFatalMask = kStatusNeighborOverflow | kStatusNotConverged,
+};
+
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float ffma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
+
+// Squared length, fused as the compiled reference expression
+// dx*dx + dy*dy + dz*dz (src/pbf/neighbors.cu:338-342).
+__device__ __forceinline__ float dist2(float dx, float dy, float dz) {
+    return ffma(dz, dz, ffma(dx, dx, fmul(dy, dy)));
+}
+__device__ __forceinline__ float len3(float x, float y, float z) { return fsqrt(dist2(x, y, z)); }
+// a.y*b.z - a.z*b.y with one rounding of the first product.
+__device__ __forceinline__ float crossc(float ay, float az, float by, float bz) {
+    return ffma(ay, bz, -fmul(az, by));
+}
+
+// Smoothing-kernel constants, computed on the host in float with the same
+// operation order as the oracle.
+struct KernelConst {
+    float h, h2, inv_h, inv_h2, c_poly6, c_spiky;
+};
+
+__host__ inline KernelConst make_kernel_const(float h) {
+    KernelConst k;
+    k.h = h;
+    k.h2 = h * h;
+    k.inv_h = 1.0f / h;
+    k.inv_h2 = 1.0f / k.h2;
+    k.c_poly6 = 315.0f / (64.0f * kPi) / h / h / h;
+    k.c_spiky = -45.0f / kPi / h / h / h / h;
+    return k;
+}
+
+// poly6FromDistanceSquared (include/pbf/sph_helpers.cuh:13-34).
+__device__ __forceinline__ float poly6(const KernelConst& k, float d2) {
+    if (d2 >= k.h2) return 0.0f;
+    const float t = ffma(-d2, k.inv_h2, 1.0f);
+    const float t2 = fmul(t, t);
+    const float t3 = fmul(t2, t);
+    return fmul(k.c_poly6, t3);
+}
+
+// spikyGradientFromDistanceSquared (include/pbf/sph_helpers.cuh:48-81).
+__device__ __forceinline__ void spiky(const KernelConst& k, float dx, float dy, float dz,
+                                      float d2, float& gx, float& gy, float& gz) {
+    const float r = fsqrt(d2);
+    if (r <= 0.0f || r >= k.h) {
+        gx = gy = gz = 0.0f;
+        return;
+    }
+    const float inv_r = fdiv(1.0f, r);
+    const float t = ffma(-r, k.inv_h, 1.0f);
+    const float mag = fmul(k.c_spiky, fmul(t, t));
+    gx = fmul(fmul(dx, inv_r), mag);
+    gy = fmul(fmul(dy, inv_r), mag);
+    gz = fmul(fmul(dz, inv_r), mag);
+}
+
+// Artificial pressure s_corr = -k (W(r)/W(dq))^n with the poly6 normalisation
+// cancelled (include/pbf/pbf_solver_kernels.cuh:24-47); the integer power is
+// taken by squaring instead of powf.
+struct ScorrConst {
+    float k, negk, h2, dq2, inv_den;
+    int n;
+};
+
+__host__ inline ScorrConst make_scorr_const(float h, float k, int n, float dq) {
+    ScorrConst s;
+    s.k = k;
+    s.negk = -k;
+    s.n = n;
+    s.h2 = h * h;
+    s.dq2 = dq * dq;
+    s.inv_den = 1.0f / (s.h2 - s.dq2);
+    return s;
+}
+
+__device__ __forceinline__ float ipow(float b, int n) {
+    float r = 1.0f;
+    while (n > 0) {
+        if (n & 1) r = fmul(r, b);
+        n >>= 1;
+        if (n) b = fmul(b, b);
+    }
+    return r;
+}
+
+__device__ __forceinline__ float scorr(const ScorrConst& s, float d2) {
+    if (s.k == 0.0f || s.n <= 0) return 0.0f;
+    if (d2 >= s.h2 || s.dq2 >= s.h2) return 0.0f;
+    const float ratio = fmul(fsub(s.h2, d2), s.inv_den);
+    const float r3 = fmul(fmul(ratio, ratio), ratio);
+    return fmul(s.negk, ipow(r3, s.n));
+}
+
+// Grid geometry: cell = floor((p - min) / cellSize) per axis with an IEEE
+// divide, saturating float->int conversion, clamp, u64 key arithmetic
+// truncated to u32 (include/pbf/spatial_grid.cuh:65-102).
+struct GridConst {
+    float minx, miny, minz, cell;
+    int gx, gy, gz;
+    int radius;  // ceil(h / cellSize), clamped to the largest grid dimension
+};
+
+__device__ __forceinline__ void cell_of(const GridConst& g, float px, float py, float pz,
+                                        int& cx, int& cy, int& cz) {
+    cx = __float2int_rz(floorf(fdiv(fsub(px, g.minx), g.cell)));
+    cy = __float2int_rz(floorf(fdiv(fsub(py, g.miny), g.cell)));
+    cz = __float2int_rz(floorf(fdiv(fsub(pz, g.minz), g.cell)));
+    cx = max(0, min(cx, g.gx - 1));
+    cy = max(0, min(cy, g.gy - 1));
+    cz = max(0, min(cz, g.gz - 1));
+}
+
+__device__ __forceinline__ uint32_t cell_key(const GridConst& g, int cx, int cy, int cz) {
+    return static_cast<uint32_t>(static_cast<uint64_t>(cx) +
+                                 static_cast<uint64_t>(cy) * static_cast<uint64_t>(g.gx) +
+                                 static_cast<uint64_t>(cz) * static_cast<uint64_t>(g.gx) *
+                                     static_cast<uint64_t>(g.gy));
+}
+
+__device__ __forceinline__ uint32_t key_of(const GridConst& g, float4 p) {
+    int cx, cy, cz;
+    cell_of(g, p.x, p.y, p.z, cx, cy, cz);
+    return cell_key(g, cx, cy, cz);
+}
+
+}  // namespace pbf

@@ -1,0 +1,233 @@
+/*
+ * pbf103.h -- C ABI of the GB300-native Position Based Fluids step.
+ *
+ * Drop-in boundary for the reference solver API of DusanCojic/Fluid-Simulator
+ * (class PBFSolver, include/pbf/pbf_solver.hpp:13-70).  Every entry point takes
+ * plain pointers and sizes and returns a pbf_status whose values map 1:1 onto
+ * the C++ exception types the reference throws; pbf_last_error() gives the
+ * message.  The header-only C++ shim include/pbf103/pbf_solver.hpp rethrows
+ * them as those exception types.
+ *
+ * Threading: one solver handle must not be used from two threads at once
+ * (the reference class is not thread-safe either).  Every call that returns
+ * data to the host is synchronous; pbf_step/pbf_run are synchronous too, like
+ * PBFSolver::step (src/pbf/pbf_solver.cu:327).
+ */
+#ifndef PBF103_H
+#define PBF103_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes <-> exception types thrown by the reference. */
+typedef enum pbf_status {
+    PBF_OK = 0,
+    PBF_ERR_INVALID_ARGUMENT = 1, /* std::invalid_argument */
+    PBF_ERR_LOGIC = 2,            /* std::logic_error (use before initialize) */
+    PBF_ERR_OUT_OF_RANGE = 3,     /* std::out_of_range */
+    PBF_ERR_LENGTH = 4,           /* std::length_error */
+    PBF_ERR_OVERFLOW = 5,         /* std::overflow_error (neighbour capacity) */
+    PBF_ERR_RUNTIME = 6           /* std::runtime_error (CUDA error, collisions did not converge) */
+} pbf_status;
+
+typedef struct pbf_float3 { float x, y, z; } pbf_float3;
+typedef struct pbf_float4 { float x, y, z, w; } pbf_float4;
+
+/* Field-for-field the layout of SimulationParams
+ * (include/pbf/simulation_params.hpp:6-29). */
+typedef struct pbf_params {
+    float dt;
+    float restDensity;
+    float particleMass;
+    float particleRadius;
+    float collisionRestitution;
+    float collisionFriction;
+    float smoothingRadius;
+    float lambdaEpsilon;
+    int solverIterations;
+    int substeps;
+    pbf_float3 gravity;
+    float scorrK;
+    int scorrN;
+    float scorrDeltaQ;
+    float xsphViscosity;
+    float vorticityStrength;
+} pbf_params;
+
+/* Collider layouts of include/pbf/colliders.hpp:8-24. */
+typedef struct pbf_sphere { pbf_float3 center; float radius; } pbf_sphere;
+typedef struct pbf_box { pbf_float3 center; pbf_float3 halfExtents; } pbf_box;
+typedef struct pbf_plane { pbf_float3 point; pbf_float3 normal; } pbf_plane;
+
+typedef struct pbf_solver pbf_solver;
+
+/* ---- solver lifetime ----------------------------------------------------
+ * Replaces PBFSolver's constructor/destructor.  create selects CUDA device
+ * `device` (-1 = the current device). */
+pbf_status pbf_solver_create(pbf_solver** out, int device);
+void pbf_solver_destroy(pbf_solver* s);
+/* Message of the last failed call on this handle ("" when none). */
+const char* pbf_last_error(const pbf_solver* s);
+/* Message of the last failed call that had no handle (create, stage calls). */
+const char* pbf_global_last_error(void);
+
+/* PBFSolver::initialize (src/pbf/pbf_solver.cu:23-116): validation, grid with
+ * cell size = smoothingRadius, container = grid bounds, capacity, and the
+ * neighbour capacity kMaxNeighbors = 256 (src/pbf/pbf_solver.cu:12). */
+pbf_status pbf_initialize(pbf_solver* s, size_t max_particles, pbf_float3 min_bounds,
+                          pbf_float3 max_bounds, const pbf_params* params);
+/* Same with an explicit neighbour capacity (the reference hard-codes 256). */
+pbf_status pbf_initialize_ex(pbf_solver* s, size_t max_particles, pbf_float3 min_bounds,
+                             pbf_float3 max_bounds, const pbf_params* params,
+                             int max_neighbors);
+
+/* PBFSolver::setParticles (src/pbf/pbf_solver.cu:118-152): host arrays,
+ * finiteness checked, stable ids reset to the given order. */
+pbf_status pbf_set_particles(pbf_solver* s, const pbf_float4* positions,
+                             const pbf_float4* velocities, size_t count);
+/* Same from device pointers (float4 arrays already resident in HBM). */
+pbf_status pbf_set_particles_device(pbf_solver* s, const pbf_float4* d_positions,
+                                    const pbf_float4* d_velocities, size_t count);
+
+/* PBFSolver::setSpheres/setBoxes/setPlanes -> CollisionSystem setters
+ * (src/pbf/collision_system.cu:53-131); count 0 clears. */
+pbf_status pbf_set_spheres(pbf_solver* s, const pbf_sphere* spheres, size_t count);
+pbf_status pbf_set_boxes(pbf_solver* s, const pbf_box* boxes, size_t count);
+pbf_status pbf_set_planes(pbf_solver* s, const pbf_plane* planes, size_t count);
+
+/* PBFSolver::step (src/pbf/pbf_solver.cu:186-328): one frame of
+ * params.substeps substeps; synchronous. */
+pbf_status pbf_step(pbf_solver* s);
+/* PBFSolver::run() / run(frameCount) (src/pbf/pbf_solver.cu:330-343).  The
+ * frames are launched back to back and checked once at the end; a failing
+ * frame stops every later kernel, so the error is the first one. */
+pbf_status pbf_run(pbf_solver* s, size_t frames);
+
+/* PBFSolver::copyPositionsToHost / copyVelocitiesToHost
+ * (src/pbf/pbf_solver.cu:345-379): API order, count must equal the active
+ * count. */
+pbf_status pbf_copy_positions(pbf_solver* s, pbf_float4* positions, size_t count);
+pbf_status pbf_copy_velocities(pbf_solver* s, pbf_float4* velocities, size_t count);
+/* Same into device memory. */
+pbf_status pbf_copy_positions_device(pbf_solver* s, pbf_float4* d_positions, size_t count);
+pbf_status pbf_copy_velocities_device(pbf_solver* s, pbf_float4* d_velocities, size_t count);
+
+size_t pbf_particle_count(const pbf_solver* s);
+
+/* ---- streams, timing, diagnostics (no counterpart in the reference) ----- */
+/* Run subsequent work on `stream` (a cudaStream_t); NULL restores the solver's
+ * own stream.  The solver still synchronises its own calls. */
+pbf_status pbf_set_stream(pbf_solver* s, void* stream);
+/* Launch `frames` frames without synchronising; returns immediately. */
+pbf_status pbf_run_async(pbf_solver* s, size_t frames);
+/* Wait for queued work and report the device status of that work. */
+pbf_status pbf_synchronize(pbf_solver* s);
+/* Time `frames` frames with CUDA events on the solver's stream. */
+pbf_status pbf_time_frames(pbf_solver* s, size_t frames, float* milliseconds);
+/* Kernel launches one frame enqueues (graph nodes that run kernels). */
+pbf_status pbf_kernels_per_frame(pbf_solver* s, int* kernels);
+/* Runs one frame with CUDA events between its stages (a second captured
+ * graph) and returns per-stage device milliseconds and launch counts, indexed
+ * by stage id 0 .. pbf_stage_count()-1; the frame advances the simulation. */
+pbf_status pbf_profile_frame(pbf_solver* s, float* stage_milliseconds, int* stage_launches);
+int pbf_stage_count(void);
+const char* pbf_stage_name(int stage);
+/* Mean and max |rho/rho0 - 1| over the current particles and the neighbour
+ * lists of the last rebuild (rho is computed but never exposed by the
+ * reference, src/pbf/pbf_solver_kernels.cu:50-75). */
+pbf_status pbf_density_error(pbf_solver* s, double* mean_error, double* max_error);
+/* Working-order snapshot: positions, stable ids and neighbour counts in the
+ * solver's current spatial order (any pointer may be NULL). */
+pbf_status pbf_copy_working_state(pbf_solver* s, pbf_float4* positions, uint32_t* ids,
+                                  int* neighbor_counts, size_t count);
+
+/* ---- stage entry points (host arrays in and out) --------------------------
+ * The reference's tests drive its kernels one by one; these mirror those
+ * kernels with the same arguments, run the corresponding device code of this
+ * library and copy the results back. */
+
+/* SpatialGrid::initialize dims + SpatialGrid::build
+ * (src/pbf/spatial_grid.cu:10-97, :139-226): stable sort of the given order
+ * by cell key, cell_start/cell_end with -1 for empty cells (num_cells =
+ * dims[0]*dims[1]*dims[2] entries each). */
+pbf_status pbf_grid_dims(pbf_float3 min_bounds, pbf_float3 max_bounds, float cell_size,
+                         int dims[3]);
+pbf_status pbf_grid_build(const pbf_float4* positions, size_t count, pbf_float3 min_bounds,
+                          pbf_float3 max_bounds, float cell_size, uint32_t* sorted_keys,
+                          uint32_t* sorted_indices, int* cell_start, int* cell_end);
+
+/* findNeighbors (src/pbf/neighbors.cu:3-91) over positions already in grid
+ * order: slot-major lists neighbors[slot*stride + i]; overflow set to 1 when
+ * any count exceeds max_neighbors. */
+pbf_status pbf_find_neighbors(const pbf_float4* sorted_positions, size_t count,
+                              const int* cell_start, const int* cell_end, const int dims[3],
+                              pbf_float3 min_bounds, float cell_size, float smoothing_radius,
+                              uint32_t* neighbors, int* neighbor_counts, int max_neighbors,
+                              size_t stride, int* overflow);
+
+/* computeLambda / computeDeltaPosition (src/pbf/pbf_solver_kernels.cu:26-182). */
+pbf_status pbf_compute_lambda(const pbf_float4* positions, const uint32_t* neighbors,
+                              const int* neighbor_counts, int max_neighbors, size_t count,
+                              size_t stride, float smoothing_radius, float mass,
+                              float rest_density, float epsilon, float* lambdas);
+pbf_status pbf_compute_delta(const pbf_float4* positions, const uint32_t* neighbors,
+                             const int* neighbor_counts, int max_neighbors,
+                             const float* lambdas, size_t count, size_t stride,
+                             float smoothing_radius, float mass, float rest_density,
+                             float scorr_k, int scorr_n, float scorr_dq, pbf_float4* deltas);
+
+/* applyXsphViscosity / computeVorticity / applyVorticityConfinement
+ * (src/pbf/pbf_solver_kernels.cu:213-385). */
+pbf_status pbf_xsph(const pbf_float4* positions, const uint32_t* neighbors,
+                    const int* neighbor_counts, int max_neighbors, const pbf_float4* velocities,
+                    pbf_float4* out_velocities, size_t count, size_t stride,
+                    float smoothing_radius, float viscosity);
+pbf_status pbf_vorticity(const pbf_float4* positions, const pbf_float4* velocities,
+                         const uint32_t* neighbors, const int* neighbor_counts,
+                         int max_neighbors, size_t count, size_t stride,
+                         float smoothing_radius, pbf_float4* omega);
+pbf_status pbf_confinement(const pbf_float4* positions, const uint32_t* neighbors,
+                           const int* neighbor_counts, int max_neighbors,
+                           const pbf_float4* omega, const pbf_float4* velocities,
+                           pbf_float4* out_velocities, size_t count, size_t stride,
+                           float smoothing_radius, float dt, float strength);
+
+/* CollisionSystem::solve (src/pbf/collision_system.cu:133-172) in place;
+ * PBF_ERR_RUNTIME when 32 passes do not converge.  pbf_collision_pass runs a
+ * single projection kernel (kind 0 container, 1 spheres, 2 boxes, 3 planes,
+ * src/pbf/collision_kernels.cu:47-234) and reports whether it corrected. */
+pbf_status pbf_collide(pbf_float4* positions, size_t count, pbf_float3 container_min,
+                       pbf_float3 container_max, const pbf_sphere* spheres, size_t sphere_count,
+                       const pbf_box* boxes, size_t box_count, const pbf_plane* planes,
+                       size_t plane_count, float particle_radius);
+pbf_status pbf_collision_pass(pbf_float4* positions, size_t count, int kind,
+                              pbf_float3 container_min, pbf_float3 container_max,
+                              const pbf_sphere* spheres, size_t sphere_count,
+                              const pbf_box* boxes, size_t box_count, const pbf_plane* planes,
+                              size_t plane_count, float particle_radius, int* corrected);
+/* CollisionSystem::resolveVelocities (src/pbf/collision_system.cu:182-218). */
+pbf_status pbf_resolve_velocities(const pbf_float4* positions,
+                                  const pbf_float4* incoming_velocities,
+                                  pbf_float4* velocities, size_t count,
+                                  pbf_float3 container_min, pbf_float3 container_max,
+                                  const pbf_sphere* spheres, size_t sphere_count,
+                                  const pbf_box* boxes, size_t box_count,
+                                  const pbf_plane* planes, size_t plane_count,
+                                  float particle_radius, float restitution, float friction);
+
+/* integrate (src/pbf/integration.cu:6-32) in place on host arrays. */
+pbf_status pbf_integrate(const pbf_float4* positions, pbf_float4* predicted,
+                         pbf_float4* velocities, size_t count, float dt, pbf_float3 gravity);
+
+/* Library version string. */
+const char* pbf_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PBF103_H */

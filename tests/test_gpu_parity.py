@@ -1,0 +1,137 @@
+"""CUDA step vs the CPU oracle on identical seeded inputs.
+
+* Bit-exact against the FP32 oracle: grid keys / sort order / cell ranges,
+  neighbour lists in slot order, and whole steps (positions, velocities,
+  stable ids, working order) -- the oracle performs the kernels' operation
+  sequence with the same fused multiply-adds.
+* Within FP32 tolerance of the FP64 oracle (reference formulas in double)
+  after 1 and 10 steps, the spec accuracy check.
+"""
+
+import numpy as np
+import pytest
+
+from backends import flat
+from cases import np_keys
+
+pytestmark = pytest.mark.gpu
+
+
+def make_pair(pbf, orc, scene, max_neighbors=256):
+    pos, vel, mn, mx, prm, col = scene
+    s = pbf.PBFSolver()
+    s.initialize(len(pos), mn, mx, prm, max_neighbors)
+    if col.get("spheres"):
+        s.set_spheres(col["spheres"])
+    if col.get("boxes"):
+        s.set_boxes(col["boxes"])
+    s.set_particles(pos, vel)
+    o = orc.OracleSolver(32)
+    o.initialize(len(pos), mn, mx, prm.as_dict(), max_neighbors)
+    o.set_colliders(flat(col.get("spheres", []), 4), flat(col.get("boxes", []), 6),
+                    flat(col.get("planes", []), 6))
+    o.set_particles(pos, vel)
+    return s, o
+
+
+def assert_bitwise(a, b, what):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    same = (a.view(np.uint32) == b.view(np.uint32)) if a.dtype == np.float32 else (a == b)
+    if not same.all():
+        bad = np.argwhere(~same)
+        raise AssertionError("%s differs at %d entries, first %s: %s vs %s" % (
+            what, len(bad), bad[0], a[tuple(bad[0])], b[tuple(bad[0])]))
+
+
+@pytest.mark.parametrize("steps", [1, 10])
+def test_dam_break_16k_bit_exact_vs_fp32_oracle(pbf, scenes, orc, steps):
+    s, o = make_pair(pbf, orc, scenes.dam_break_16k())
+    s.run(steps)
+    assert o.run(steps) == 0
+    assert_bitwise(s.copy_positions_to_host(), o.positions(), "positions")
+    assert_bitwise(s.copy_velocities_to_host(), o.velocities(), "velocities")
+    wp, wid, wcnt = s.working_state()
+    op, oid, ocnt = o.working()
+    assert_bitwise(wid, oid, "working order (stable ids)")
+    assert_bitwise(wcnt, ocnt, "neighbour counts")
+    assert_bitwise(wp, op, "working positions")
+
+
+def test_reference_scene_with_colliders_bit_exact(pbf, scenes, orc):
+    """The reference benchmark's box + sphere scene (2 substeps), one 128x64 layer."""
+    scene = scenes.reference_benchmark(8192)
+    s, o = make_pair(pbf, orc, scene)
+    s.run(5)
+    assert o.run(5) == 0
+    assert_bitwise(s.copy_positions_to_host(), o.positions(), "positions")
+    assert_bitwise(s.copy_velocities_to_host(), o.velocities(), "velocities")
+
+
+@pytest.mark.parametrize("steps,tol", [(1, 2e-5), (10, 1e-3)])
+def test_dam_break_16k_vs_fp64_oracle(pbf, scenes, orc, steps, tol):
+    """Positions within `tol` (absolute, length units, h = 0.1) of the FP64
+    oracle; velocities within tol / dt."""
+    pos, vel, mn, mx, prm, col = scenes.dam_break_16k()
+    s = pbf.PBFSolver()
+    s.initialize(len(pos), mn, mx, prm)
+    s.set_particles(pos, vel)
+    s.run(steps)
+    o = orc.OracleSolver(64)
+    o.initialize(len(pos), mn, mx, prm.as_dict())
+    o.set_particles(pos, vel)
+    assert o.run(steps) == 0
+    dp = np.abs(s.copy_positions_to_host()[:, :3] - o.positions()[:, :3])
+    dv = np.abs(s.copy_velocities_to_host()[:, :3] - o.velocities()[:, :3])
+    assert np.isfinite(dp).all()
+    # Contact switches (|x - wall| < 1e-4) may flip for a handful of particles
+    # between FP32 and FP64; bound the bulk by tol and the tail loosely.
+    assert np.percentile(dp, 99.9) <= tol, np.percentile(dp, 99.9)
+    assert np.percentile(dv, 99.9) <= tol * 60.0, np.percentile(dv, 99.9)
+    assert dp.max() <= 50 * tol
+
+
+def test_grid_build_bit_exact_at_1m(pbf, scenes):
+    """Hash, stable sort and ranges of 1,048,576 particles against the numpy
+    restatement of the reference's buildReference."""
+    pos, _, mn, mx, prm, _ = scenes.dam_break_1m()
+    rng = np.random.default_rng(3)
+    pos = pos.copy()
+    pos[:, :3] += rng.normal(0, 0.02, (len(pos), 3)).astype(np.float32)
+    got = pbf.grid_build(pos, mn, mx, prm.smoothingRadius)
+    dims = pbf.grid_dims(mn, mx, prm.smoothingRadius)
+    # Vectorised restatement of buildReference (cases.np_build loops in Python).
+    keys = np_keys(pos, mn, prm.smoothingRadius, dims)
+    idx = np.argsort(keys, kind="stable").astype(np.uint32)
+    sk = keys[idx]
+    np.testing.assert_array_equal(got[0], sk)
+    np.testing.assert_array_equal(got[1], idx)
+    cells = dims[0] * dims[1] * dims[2]
+    starts = np.full(cells, -1, np.int64)
+    ends = np.full(cells, -1, np.int64)
+    first = np.ones(len(sk), bool)
+    first[1:] = sk[1:] != sk[:-1]
+    last = np.ones(len(sk), bool)
+    last[:-1] = sk[1:] != sk[:-1]
+    starts[sk[first]] = np.nonzero(first)[0]
+    ends[sk[last]] = np.nonzero(last)[0] + 1
+    np.testing.assert_array_equal(got[2], starts)
+    np.testing.assert_array_equal(got[3], ends)
+
+
+def test_neighbor_lists_bit_exact_vs_oracle_slot_order(pbf, scenes, orc):
+    """Slot-major lists in walk order, identical to the oracle's findNeighbors."""
+    pos, _, mn, mx, prm, _ = scenes.dam_break_16k()
+    h = prm.smoothingRadius
+    sk, si, cs, ce = pbf.grid_build(pos, mn, mx, h)
+    dims = pbf.grid_dims(mn, mx, h)
+    sp = pos[si]
+    nb, cnt, ov = pbf.find_neighbors(sp, cs, ce, dims, mn, h, h, 256, len(sp))
+    onb, ocnt, oov = orc.find_neighbors(sp, cs, ce, dims, mn, h, h, 256, len(sp))
+    assert not ov and not oov
+    assert_bitwise(cnt, ocnt, "counts")
+    kmax = int(cnt.max())
+    n = len(sp)
+    for k in range(kmax):
+        used = cnt > k
+        assert_bitwise(nb[k * n:(k + 1) * n][used], onb[k * n:(k + 1) * n][used], "slot %d" % k)
