@@ -260,6 +260,8 @@ def main():
     ap.add_argument("--scene", default="dam_break_1m")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--max-neighbors", type=int, default=256,
+                    help="neighbour list capacity (the reference fixes 256)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -275,7 +277,7 @@ def main():
     n = len(pos)
 
     s = pkg.PBFSolver(local)
-    s.initialize(n, mn, mx, prm)
+    s.initialize(n, mn, mx, prm, args.max_neighbors)
     for k, fn in (("spheres", s.set_spheres), ("boxes", s.set_boxes), ("planes", s.set_planes)):
         if col.get(k):
             fn(col[k])
@@ -354,6 +356,7 @@ def main():
             "data": "synthetic: seeded 128x128x64 dam-break lattice (no dataset)",
             "config": {"workload": WORKLOAD if args.scene == "dam_break_1m" else args.scene,
                        "particles": n, "iterations": prm.solverIterations,
+                       "max_neighbors": args.max_neighbors,
                        "substeps": prm.substeps, "parallelism": "replicas" if world > 1 else
                        "single GPU", "l2": "step working set ~250 MB > 129 MB L2 (no flush)",
                        "timing": "CUDA events around %d graph-replayed steps on the solver "

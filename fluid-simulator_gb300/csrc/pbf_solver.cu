@@ -73,7 +73,9 @@ struct Marks {
             stages.push_back(stage);
         }
         stages[used] = stage;
-        cuda_check(cudaEventRecord(events[used], st));
+        // External records become event nodes of the captured graph, so the
+        // events are really recorded each time the graph runs.
+        cuda_check(cudaEventRecordWithFlags(events[used], st, cudaEventRecordExternal));
         ++used;
     }
     ~Marks() {
