@@ -64,6 +64,25 @@ k_cell_ranges(const uint32_t* __restrict__ skeys, int* __restrict__ cs, int* __r
     if (i == n - 1 || skeys[i + 1] != key) ce[key] = i + 1;
 }
 
+// first[k] = lower_bound(sorted keys, k) for k in [0, cells]: the particles of
+// cells [a, b] are exactly [first[a], first[b + 1]).  Equivalent to the
+// reference's cellStart/cellEnd pair (spatial_grid.cu:123-137) with empty
+// cells resolved to the next occupied one, so a run of cells along x is one
+// contiguous index range.
+__global__ void __launch_bounds__(kBlock)
+k_cell_first(const uint32_t* __restrict__ skeys, int n, uint32_t cells, int* __restrict__ first,
+             const unsigned* __restrict__ status) {
+    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k > cells || fatal(status)) return;
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&skeys[mid]) < k) lo = mid + 1;
+        else hi = mid;
+    }
+    first[k] = lo;
+}
+
 __global__ void __launch_bounds__(kBlock)
 k_gather_xs(const uint32_t* __restrict__ perm, const float4* __restrict__ xs_in,
             float4* __restrict__ xs_out, const uint32_t* __restrict__ org_in,
@@ -106,9 +125,9 @@ __device__ __forceinline__ float lambda_finish(const StepConst& c, const LambdaA
 
 template <bool LAMBDA>
 __global__ void __launch_bounds__(kBlock)
-k_search(const float4* __restrict__ xs, const int* __restrict__ cs, const int* __restrict__ ce,
-         StepConst c, int n, uint32_t* __restrict__ nbr, int* __restrict__ cnt,
-         float* __restrict__ lam, unsigned* __restrict__ status) {
+k_search(const float4* __restrict__ xs, const int* __restrict__ first, StepConst c, int n,
+         uint32_t* __restrict__ nbr, int* __restrict__ cnt, float* __restrict__ lam,
+         unsigned* __restrict__ status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || fatal(status)) return;
     const float4 pi = xs[i];
@@ -118,62 +137,111 @@ k_search(const float4* __restrict__ xs, const int* __restrict__ cs, const int* _
     const int x0 = max(0, cx - R), x1 = min(c.g.gx - 1, cx + R);
     const int y0 = max(0, cy - R), y1 = min(c.g.gy - 1, cy + R);
     const int z0 = max(0, cz - R), z1 = min(c.g.gz - 1, cz + R);
+    // Keys fit in 32 bits (cells < 2^32 is checked at initialisation), so
+    // the reference's 64-bit key arithmetic truncates to the same values.
+    const uint32_t gx = static_cast<uint32_t>(c.g.gx);
+    const uint32_t gxy = gx * static_cast<uint32_t>(c.g.gy);
     const float h2 = c.k.h2;
-    LambdaAcc acc{c.k.c_poly6, 0.0f, 0.0f, 0.0f, 0.0f};
+    uint32_t* __restrict__ out = nbr + i;
+    const size_t stride = c.stride;
     int count = 0;
+    // Rows z -> y; inside a row the cells x0..x1 are consecutive keys, so the
+    // candidates of the row are one index range walked in ascending order --
+    // exactly the reference's z -> y -> x cell walk (neighbors.cu:319-354).
     for (int z = z0; z <= z1; ++z) {
         for (int y = y0; y <= y1; ++y) {
-            for (int x = x0; x <= x1; ++x) {
-                const uint32_t key = cell_key(c.g, x, y, z);
-                const int s = __ldg(&cs[key]);
-                if (s == -1) continue;
-                const int e = __ldg(&ce[key]);
-                for (int j = s; j < e; ++j) {
-                    if (j == i) continue;
-                    const float4 pj = __ldg(&xs[j]);
-                    const float dx = fsub(pi.x, pj.x);
-                    const float dy = fsub(pi.y, pj.y);
-                    const float dz = fsub(pi.z, pj.z);
-                    const float d2 = dist2(dx, dy, dz);
-                    if (d2 <= h2) {
-                        if (count < c.max_nb)
-                            nbr[static_cast<size_t>(count) * c.stride + i] =
-                                static_cast<uint32_t>(j);
-                        ++count;
-                        if (LAMBDA) lambda_add(c.k, acc, dx, dy, dz, d2);
-                    }
+            const uint32_t row = static_cast<uint32_t>(y) * gx + static_cast<uint32_t>(z) * gxy;
+            const int s = __ldg(&first[row + static_cast<uint32_t>(x0)]);
+            const int e = __ldg(&first[row + static_cast<uint32_t>(x1) + 1u]);
+#pragma unroll 4
+            for (int j = s; j < e; ++j) {
+                const float4 pj = __ldg(&xs[j]);
+                const float d2 = dist2(fsub(pi.x, pj.x), fsub(pi.y, pj.y), fsub(pi.z, pj.z));
+                if (d2 <= h2 && j != i) {
+                    if (count < c.max_nb) out[static_cast<size_t>(count) * stride] =
+                        static_cast<uint32_t>(j);
+                    ++count;
                 }
             }
         }
     }
     cnt[i] = count;
     if (count > c.max_nb) atomicOr(status, kStatusNeighborOverflow);
-    if (LAMBDA) lam[i] = count > c.max_nb ? CUDART_NAN_F : lambda_finish(c, acc);
+    if (LAMBDA) {
+        if (count > c.max_nb) {
+            lam[i] = CUDART_NAN_F;
+            return;
+        }
+        // Second pass over the list just written: the constraint terms run
+        // once per neighbour instead of once per candidate in which any lane
+        // of the warp hit.  Same order as the list, so the same sums.
+        LambdaAcc acc{c.k.c_poly6, 0.0f, 0.0f, 0.0f, 0.0f};
+        for (int k = 0; k < count; ++k) {
+            const float4 pj = __ldg(&xs[out[static_cast<size_t>(k) * stride]]);
+            const float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y), dz = fsub(pi.z, pj.z);
+            lambda_add(c.k, acc, dx, dy, dz, dist2(dx, dy, dz));
+        }
+        lam[i] = lambda_finish(c, acc);
+    }
 }
 
 __device__ __forceinline__ bool count_ok(int count, int max_nb) {
     return count >= 0 && count <= max_nb;
 }
 
+// Walks a slot-major list in order, B neighbours at a time: the B indices,
+// then the B gathers (load(j)), are issued before any use(), so dependent
+// loads overlap while every use() still runs in list order.
+template <int B, class T, class Load, class Use>
+__device__ __forceinline__ void for_each_neighbor(const uint32_t* __restrict__ row, size_t stride,
+                                                  int count, Load load, Use use) {
+    int k = 0;
+    for (; k + B <= count; k += B) {
+        uint32_t j[B];
+        T v[B];
+#pragma unroll
+        for (int b = 0; b < B; ++b) j[b] = __ldg(&row[static_cast<size_t>(k + b) * stride]);
+#pragma unroll
+        for (int b = 0; b < B; ++b) v[b] = load(j[b]);
+#pragma unroll
+        for (int b = 0; b < B; ++b) use(v[b]);
+    }
+    for (; k < count; ++k) use(load(__ldg(&row[static_cast<size_t>(k) * stride])));
+}
+
+struct PosVel {
+    float4 p, v;
+};
+struct PosLam {
+    float4 p;
+    float l;
+};
+
 // computeDeltaPosition summed in list order (pbf_solver_kernels.cu:134-171).
+// Indices, positions and lambdas of four neighbours are loaded before any of
+// them is used, so the dependent gathers overlap; the sum stays in list order.
+__device__ __forceinline__ void delta_term(const StepConst& c, float4 pi, float li, float4 pj,
+                                           float lj, float& ax, float& ay, float& az) {
+    const float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y), dz = fsub(pi.z, pj.z);
+    const float d2 = dist2(dx, dy, dz);
+    float gx, gy, gz;
+    spiky(c.k, dx, dy, dz, d2, gx, gy, gz);
+    const float ls = fadd(fadd(li, lj), scorr(c.sc, d2));
+    ax = ffma(ls, gx, ax);
+    ay = ffma(ls, gy, ay);
+    az = ffma(ls, gz, az);
+}
+
 __device__ __forceinline__ void delta_sum(const StepConst& c, const float4* __restrict__ xs,
                                           const uint32_t* __restrict__ nbr,
                                           const float* __restrict__ lam, int i, int count,
                                           float4 pi, float& dpx, float& dpy, float& dpz) {
     const float li = lam[i];
     float ax = 0.0f, ay = 0.0f, az = 0.0f;
-    for (int k = 0; k < count; ++k) {
-        const uint32_t j = __ldg(&nbr[static_cast<size_t>(k) * c.stride + i]);
-        const float4 pj = __ldg(&xs[j]);
-        const float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y), dz = fsub(pi.z, pj.z);
-        const float d2 = dist2(dx, dy, dz);
-        float gx, gy, gz;
-        spiky(c.k, dx, dy, dz, d2, gx, gy, gz);
-        const float ls = fadd(fadd(li, __ldg(&lam[j])), scorr(c.sc, d2));
-        ax = ffma(ls, gx, ax);
-        ay = ffma(ls, gy, ay);
-        az = ffma(ls, gz, az);
-    }
+    for_each_neighbor<4, PosLam>(
+        nbr + i, c.stride, count,
+        [&](uint32_t j) { return PosLam{__ldg(&xs[j]), __ldg(&lam[j])}; },
+        [&](const PosLam& q) { delta_term(c, pi, li, q.p, q.l, ax, ay, az); });
     dpx = fmul(c.gs, ax);
     dpy = fmul(c.gs, ay);
     dpz = fmul(c.gs, az);
@@ -236,15 +304,16 @@ __device__ __forceinline__ float4 xsph_one(const StepConst& c, const float4* __r
         return make_float4(CUDART_NAN_F, CUDART_NAN_F, CUDART_NAN_F, vi.w);
     const float4 pi = x[i];
     float cx = 0.0f, cy = 0.0f, cz = 0.0f;
-    for (int k = 0; k < count; ++k) {
-        const uint32_t j = __ldg(&nbr[static_cast<size_t>(k) * c.stride + i]);
-        const float4 pj = __ldg(&x[j]);
-        const float4 vj = __ldg(&v[j]);
-        const float w = poly6(c.k, dist2(fsub(pi.x, pj.x), fsub(pi.y, pj.y), fsub(pi.z, pj.z)));
-        cx = ffma(fsub(vj.x, vi.x), w, cx);
-        cy = ffma(fsub(vj.y, vi.y), w, cy);
-        cz = ffma(fsub(vj.z, vi.z), w, cz);
-    }
+    for_each_neighbor<4, PosVel>(
+        nbr + i, c.stride, count,
+        [&](uint32_t j) { return PosVel{__ldg(&x[j]), __ldg(&v[j])}; },
+        [&](const PosVel& q) {
+            const float w =
+                poly6(c.k, dist2(fsub(pi.x, q.p.x), fsub(pi.y, q.p.y), fsub(pi.z, q.p.z)));
+            cx = ffma(fsub(q.v.x, vi.x), w, cx);
+            cy = ffma(fsub(q.v.y, vi.y), w, cy);
+            cz = ffma(fsub(q.v.z, vi.z), w, cz);
+        });
     return make_float4(ffma(c.xsph_c, cx, vi.x), ffma(c.xsph_c, cy, vi.y),
                        ffma(c.xsph_c, cz, vi.z), vi.w);
 }
@@ -276,18 +345,18 @@ k_vorticity(const float4* __restrict__ x, const float4* __restrict__ v,
     }
     const float4 pi = x[i], vi = v[i];
     float ox = 0.0f, oy = 0.0f, oz = 0.0f;
-    for (int k = 0; k < count; ++k) {
-        const uint32_t j = __ldg(&nbr[static_cast<size_t>(k) * c.stride + i]);
-        const float4 pj = __ldg(&x[j]);
-        const float4 vj = __ldg(&v[j]);
-        const float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y), dz = fsub(pi.z, pj.z);
-        float gx, gy, gz;
-        spiky(c.k, dx, dy, dz, dist2(dx, dy, dz), gx, gy, gz);
-        const float vx = fsub(vj.x, vi.x), vy = fsub(vj.y, vi.y), vz = fsub(vj.z, vi.z);
-        ox = fadd(ox, crossc(gy, gz, vy, vz));
-        oy = fadd(oy, crossc(gz, gx, vz, vx));
-        oz = fadd(oz, crossc(gx, gy, vx, vy));
-    }
+    for_each_neighbor<4, PosVel>(
+        nbr + i, c.stride, count,
+        [&](uint32_t j) { return PosVel{__ldg(&x[j]), __ldg(&v[j])}; },
+        [&](const PosVel& q) {
+            const float dx = fsub(pi.x, q.p.x), dy = fsub(pi.y, q.p.y), dz = fsub(pi.z, q.p.z);
+            float gx, gy, gz;
+            spiky(c.k, dx, dy, dz, dist2(dx, dy, dz), gx, gy, gz);
+            const float vx = fsub(q.v.x, vi.x), vy = fsub(q.v.y, vi.y), vz = fsub(q.v.z, vi.z);
+            ox = fadd(ox, crossc(gy, gz, vy, vz));
+            oy = fadd(oy, crossc(gz, gx, vz, vx));
+            oz = fadd(oz, crossc(gx, gy, vx, vy));
+        });
     omega[i] = make_float4(ox, oy, oz, 0.0f);
 }
 
@@ -302,19 +371,19 @@ __device__ __forceinline__ float4 confine_one(const StepConst& c, const float4* 
     const float4 pi = x[i], wi = om[i];
     const float wil = len3(wi.x, wi.y, wi.z);
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
-    for (int k = 0; k < count; ++k) {
-        const uint32_t j = __ldg(&nbr[static_cast<size_t>(k) * c.stride + i]);
-        const float4 pj = __ldg(&x[j]);
-        const float4 wj = __ldg(&om[j]);
-        const float wjl = len3(wj.x, wj.y, wj.z);
-        const float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y), dz = fsub(pi.z, pj.z);
-        float gx, gy, gz;
-        spiky(c.k, dx, dy, dz, dist2(dx, dy, dz), gx, gy, gz);
-        const float md = fsub(wjl, wil);
-        ex = ffma(md, gx, ex);
-        ey = ffma(md, gy, ey);
-        ez = ffma(md, gz, ez);
-    }
+    for_each_neighbor<4, PosVel>(
+        nbr + i, c.stride, count,
+        [&](uint32_t j) { return PosVel{__ldg(&x[j]), __ldg(&om[j])}; },
+        [&](const PosVel& q) {
+            const float wjl = len3(q.v.x, q.v.y, q.v.z);
+            const float dx = fsub(pi.x, q.p.x), dy = fsub(pi.y, q.p.y), dz = fsub(pi.z, q.p.z);
+            float gx, gy, gz;
+            spiky(c.k, dx, dy, dz, dist2(dx, dy, dz), gx, gy, gz);
+            const float md = fsub(wjl, wil);
+            ex = ffma(md, gx, ex);
+            ey = ffma(md, gy, ey);
+            ez = ffma(md, gz, ez);
+        });
     const float el = len3(ex, ey, ez);
     float nx = 0.0f, ny = 0.0f, nz = 0.0f;
     if (el > kEtaEpsilon) {
@@ -466,18 +535,22 @@ void launch_cell_ranges(const uint32_t* skeys, int* cs, int* ce, int n, const un
                         cudaStream_t st) {
     k_cell_ranges<<<blocks_for(n), kBlock, 0, st>>>(skeys, cs, ce, n, status);
 }
+void launch_cell_first(const uint32_t* skeys, int n, uint64_t cells, int* first,
+                       const unsigned* status, cudaStream_t st) {
+    k_cell_first<<<blocks_for(cells + 1), kBlock, 0, st>>>(skeys, n, static_cast<uint32_t>(cells),
+                                                           first, status);
+}
 void launch_gather_xs(const uint32_t* perm, const float4* xs_in, float4* xs_out,
                       const uint32_t* org_in, uint32_t* org_out, int n, const unsigned* status,
                       cudaStream_t st) {
     k_gather_xs<<<blocks_for(n), kBlock, 0, st>>>(perm, xs_in, xs_out, org_in, org_out, n, status);
 }
-void launch_search(const float4* xs, const int* cs, const int* ce, const StepConst& c, int n,
-                   uint32_t* nbr, int* cnt, float* lam, unsigned* status, bool with_lambda,
-                   cudaStream_t st) {
+void launch_search(const float4* xs, const int* first, const StepConst& c, int n, uint32_t* nbr,
+                   int* cnt, float* lam, unsigned* status, bool with_lambda, cudaStream_t st) {
     if (with_lambda)
-        k_search<true><<<blocks_for(n), kBlock, 0, st>>>(xs, cs, ce, c, n, nbr, cnt, lam, status);
+        k_search<true><<<blocks_for(n), kBlock, 0, st>>>(xs, first, c, n, nbr, cnt, lam, status);
     else
-        k_search<false><<<blocks_for(n), kBlock, 0, st>>>(xs, cs, ce, c, n, nbr, cnt, lam, status);
+        k_search<false><<<blocks_for(n), kBlock, 0, st>>>(xs, first, c, n, nbr, cnt, lam, status);
 }
 void launch_delta_apply(const float4* xs, const uint32_t* nbr, const int* cnt, const float* lam,
                         const StepConst& c, int n, float4* xs_out, uint32_t* keys_out,

@@ -153,7 +153,7 @@ struct pbf_solver {
     DeviceBuffer f4[kF4Pool];
     DeviceBuffer ids[2], org[2];
     DeviceBuffer keys, skeys, sidx, akeys, aidx;
-    DeviceBuffer cell_start, cell_end, nbr, cnt, lam, sort_scratch, status, tmp4, ftmp;
+    DeviceBuffer cell_first, nbr, cnt, lam, sort_scratch, status, tmp4, ftmp;
     unsigned* h_status = nullptr;
     int ix = 0, iv = 1, iid = 0;  // roles: positions, velocities, ids
 
@@ -289,10 +289,7 @@ struct pbf_solver {
                 launch_sort(plan, keys.as<uint32_t>(), skeys.as<uint32_t>(), sidx.as<uint32_t>(),
                             akeys.as<uint32_t>(), aidx.as<uint32_t>(), sort_scratch.get(), sp, st);
                 M(kStRanges);
-                cuda_check(cudaMemsetAsync(cell_start.get(), 0xff, cells * sizeof(int), st));
-                cuda_check(cudaMemsetAsync(cell_end.get(), 0xff, cells * sizeof(int), st));
-                launch_cell_ranges(skeys.as<uint32_t>(), cell_start.as<int>(), cell_end.as<int>(),
-                                   N, sp, st);
+                launch_cell_first(skeys.as<uint32_t>(), N, cells, cell_first.as<int>(), sp, st);
                 const int nxt = take();
                 const int org_next = org_cur < 0 ? 0 : 1 - org_cur;
                 M(kStGather);
@@ -306,8 +303,8 @@ struct pbf_solver {
             for (int it = 0; it < prm.solverIterations; ++it) {
                 rebuild();
                 M(kStSearchLambda);
-                launch_search(P(cur), cell_start.as<int>(), cell_end.as<int>(), c, N,
-                              nbr.as<uint32_t>(), cnt.as<int>(), lam.as<float>(), sp, true, st);
+                launch_search(P(cur), cell_first.as<int>(), c, N, nbr.as<uint32_t>(),
+                              cnt.as<int>(), lam.as<float>(), sp, true, st);
                 const int nxt = take();
                 M(kStDeltaApply);
                 launch_delta_apply(P(cur), nbr.as<uint32_t>(), cnt.as<int>(), lam.as<float>(), c,
@@ -318,8 +315,8 @@ struct pbf_solver {
             if (post) {
                 rebuild();
                 M(kStSearch);
-                launch_search(P(cur), cell_start.as<int>(), cell_end.as<int>(), c, N,
-                              nbr.as<uint32_t>(), cnt.as<int>(), nullptr, sp, false, st);
+                launch_search(P(cur), cell_first.as<int>(), c, N, nbr.as<uint32_t>(),
+                              cnt.as<int>(), nullptr, sp, false, st);
             }
             const int vnew = take();
             const int vinnew = take();
@@ -496,7 +493,7 @@ struct pbf_solver {
         for (auto& b : nids) b.allocate(u4b);
         for (auto& b : norg) b.allocate(u4b);
         DeviceBuffer nkeys(u4b), nskeys(u4b), nsidx(u4b), nakeys(u4b), naidx(u4b);
-        DeviceBuffer ncs(ncells * sizeof(int)), nce(ncells * sizeof(int));
+        DeviceBuffer nfirst((ncells + 1) * sizeof(int));
         DeviceBuffer nnbr(strd * size_t(maxnb) * sizeof(uint32_t));
         DeviceBuffer ncnt(u4b), nlam(u4b), nscr(sort_scratch_bytes(int(max_particles)));
         DeviceBuffer nstat(sizeof(unsigned)), ntmp(f4b), nftmp(u4b);
@@ -512,8 +509,7 @@ struct pbf_solver {
         sidx = std::move(nsidx);
         akeys = std::move(nakeys);
         aidx = std::move(naidx);
-        cell_start = std::move(ncs);
-        cell_end = std::move(nce);
+        cell_first = std::move(nfirst);
         nbr = std::move(nnbr);
         cnt = std::move(ncnt);
         lam = std::move(nlam);

@@ -197,15 +197,22 @@ pbf_status pbf_find_neighbors(const pbf_float4* sorted_positions, size_t count,
         const size_t cells = size_t(dims[0]) * size_t(dims[1]) * size_t(dims[2]);
         const size_t list = stride * size_t(max_neighbors);
         need(neighbors, list, "neighbors must not be null");
+        need(cell_start, cells, "cell_start must not be null");
+        need(cell_end, cells, "cell_end must not be null");
+        // cellStart/cellEnd -> lower bound of every key (empty cells take the
+        // next occupied cell's start), the table the search kernel walks.
+        std::vector<int> first(cells + 1);
+        first[cells] = static_cast<int>(count);
+        for (size_t k = cells; k-- > 0;) first[k] = cell_start[k] != -1 ? cell_start[k] : first[k + 1];
         DeviceBuffer dpos = upload(reinterpret_cast<const float4*>(sorted_positions), count);
-        DeviceBuffer dcs = upload(cell_start, cells), dce = upload(cell_end, cells);
+        DeviceBuffer dfirst = upload(first.data(), first.size());
         DeviceBuffer dnb = upload(neighbors, list);  // untouched slots keep caller values
         DeviceBuffer dcnt(count * sizeof(int)), dstat(sizeof(unsigned));
         cuda_check(cudaMemset(dstat.get(), 0, sizeof(unsigned)));
         StepConst c = kernel_const(h, 1.0f, 1.0f, max_neighbors, stride);
         c.k.h2 = h * h;
         c.g = grid_const(mn, cell, dims, h);
-        launch_search(dpos.as<float4>(), dcs.as<int>(), dce.as<int>(), c, static_cast<int>(count),
+        launch_search(dpos.as<float4>(), dfirst.as<int>(), c, static_cast<int>(count),
                       dnb.as<uint32_t>(), dcnt.as<int>(), nullptr, dstat.as<unsigned>(), false,
                       nullptr);
         cuda_check(cudaGetLastError());
