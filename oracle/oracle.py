@@ -370,3 +370,159 @@ class OracleSolver:
         x = C.c_double()
         lib().orc_solver_density_error(self._h, C.byref(m), C.byref(x))
         return m.value, x.value
+
+
+# ---- the reference's own CUDA kernels (GPU comparison point) -----------------
+#
+# oracle/build_ref.py compiles the reference's kernel sources into fatbins in
+# oracle/_ref/; ref_driver.cu (restated PBFSolver host orchestration) launches
+# them.  Used by tests/ and bench.py only, as the checker and as the
+# "reference CUDA solver" timing; never by the product.
+
+REF_DIR = os.path.join(HERE, "_ref")
+REF_DRIVER_SRC = os.path.join(HERE, "ref_driver.cu")
+REF_DRIVER = os.path.join(BUILD_DIR, "libref_driver.so")
+REF_OK, REF_ERR, REF_OVERFLOW, REF_NOT_CONVERGED = range(4)
+
+
+def ref_fatbins_available() -> bool:
+    from oracle import build_ref
+    return build_ref.available()
+
+
+def build_ref_driver(force: bool = False) -> str:
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    if (not force and os.path.exists(REF_DRIVER)
+            and os.path.getmtime(REF_DRIVER) >= os.path.getmtime(REF_DRIVER_SRC)):
+        return REF_DRIVER
+    import shutil
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    cuda = os.path.dirname(os.path.dirname(os.path.realpath(nvcc)))
+    tmp = REF_DRIVER + ".tmp%d" % os.getpid()
+    subprocess.check_call([nvcc, "-O3", "-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a",
+                           "-Xcompiler", "-fPIC", "-shared", REF_DRIVER_SRC, "-o", tmp,
+                           "-L" + os.path.join(cuda, "lib64", "stubs"), "-lcuda"])
+    os.replace(tmp, REF_DRIVER)
+    return REF_DRIVER
+
+
+_ref = None
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        L = C.CDLL(build_ref_driver())
+        L.ref_last_error.restype = C.c_char_p
+        L.ref_create.argtypes = [C.c_char_p]
+        L.ref_create.restype = _vp
+        L.ref_destroy.argtypes = [_vp]
+        L.ref_initialize.argtypes = [_vp, C.c_size_t, F3, F3, C.POINTER(Params)]
+        L.ref_set_colliders.argtypes = [_vp, _vp, C.c_size_t, _vp, C.c_size_t, _vp, C.c_size_t]
+        L.ref_set_particles.argtypes = [_vp, _vp, _vp, C.c_size_t]
+        L.ref_step.argtypes = [_vp]
+        L.ref_time_steps.argtypes = [_vp, C.c_size_t, C.POINTER(C.c_double)]
+        L.ref_copy.argtypes = [_vp, C.c_int, _vp, C.c_size_t]
+        L.ref_grid_build.argtypes = [_vp, _vp, C.c_size_t, _vp, _vp, _vp, _vp]
+        L.ref_find_neighbors.argtypes = [_vp, _vp, C.c_size_t, _vp, _vp, C.POINTER(C.c_size_t)]
+        L.ref_stride.argtypes = [_vp]
+        L.ref_stride.restype = C.c_size_t
+        L.ref_num_cells.argtypes = [_vp]
+        L.ref_num_cells.restype = C.c_size_t
+        _ref = L
+    return _ref
+
+
+class RefCudaSolver:
+    """The reference's compiled kernels driven like PBFSolver (default stream,
+    per-iteration host synchronisation)."""
+
+    def __init__(self):
+        L = ref_lib()
+        self._h = L.ref_create(REF_DIR.encode())
+        if not self._h:
+            raise RuntimeError("reference kernels unavailable: " + L.ref_last_error().decode())
+        self.n = 0
+
+    def close(self):
+        if self._h:
+            ref_lib().ref_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _ok(self, st):
+        if st != REF_OK:
+            raise RuntimeError("reference solver status %d: %s" % (
+                st, ref_lib().ref_last_error().decode()))
+
+    def initialize(self, max_particles, mn, mx, params: dict):
+        self._params = params_struct(params)
+        self._ok(ref_lib().ref_initialize(self._h, max_particles, f3(mn), f3(mx),
+                                          C.byref(self._params)))
+
+    def set_colliders(self, spheres=(), boxes=(), planes=()):
+        sp, bx, pl = colliders_arrays(spheres, boxes, planes)
+        self._col = (sp, bx, pl)
+        self._ok(ref_lib().ref_set_colliders(self._h, _p(sp), sp.shape[0], _p(bx), bx.shape[0],
+                                             _p(pl), pl.shape[0]))
+
+    def set_particles(self, pos, vel):
+        pos = as_f4(pos)
+        vel = as_f4(vel)
+        self._ok(ref_lib().ref_set_particles(self._h, _p(pos), _p(vel), pos.shape[0]))
+        self.n = pos.shape[0]
+
+    def step(self) -> int:
+        return ref_lib().ref_step(self._h)
+
+    def run(self, frames) -> int:
+        for _ in range(frames):
+            st = self.step()
+            if st != REF_OK:
+                return st
+        return REF_OK
+
+    def time_steps(self, frames) -> float:
+        ms = C.c_double()
+        self._ok(ref_lib().ref_time_steps(self._h, frames, C.byref(ms)))
+        return ms.value
+
+    def positions(self):
+        out = np.zeros((self.n, 4), np.float32)
+        self._ok(ref_lib().ref_copy(self._h, 0, _p(out), self.n))
+        return out
+
+    def velocities(self):
+        out = np.zeros((self.n, 4), np.float32)
+        self._ok(ref_lib().ref_copy(self._h, 1, _p(out), self.n))
+        return out
+
+    def grid_build(self, pos):
+        pos = as_f4(pos)
+        n = pos.shape[0]
+        cells = ref_lib().ref_num_cells(self._h)
+        sk = np.zeros(n, np.uint32)
+        si = np.zeros(n, np.uint32)
+        cs = np.zeros(cells, np.int32)
+        ce = np.zeros(cells, np.int32)
+        self._ok(ref_lib().ref_grid_build(self._h, _p(pos), n, _p(sk), _p(si), _p(cs), _p(ce)))
+        return sk, si, cs, ce
+
+    def find_neighbors(self, sorted_pos):
+        """Lists of findNeighbors on positions already in grid order (the grid of
+        the last grid_build): (slot-major lists, counts, stride, overflow)."""
+        sp = as_f4(sorted_pos)
+        n = sp.shape[0]
+        stride = ref_lib().ref_stride(self._h)
+        nb = np.zeros(stride * 256, np.uint32)
+        cnt = np.zeros(n, np.int32)
+        st_out = C.c_size_t()
+        st = ref_lib().ref_find_neighbors(self._h, _p(sp), n, _p(nb), _p(cnt), C.byref(st_out))
+        if st not in (REF_OK, REF_OVERFLOW):
+            self._ok(st)
+        return nb, cnt, st_out.value, st == REF_OVERFLOW
