@@ -222,6 +222,35 @@ def cpu_baseline(scene, seconds_budget: float = 20.0, threads: int = 0):
                       "(FP32 C++/OpenMP restatement, %.1f s)" % (steps, len(pos), dt)}
 
 
+def reference_cuda(scene, steps: int, warmup: int):
+    """The reference's own kernels (compiled from its sources, Release, sm_103a)
+    driven with PBFSolver's host sequence, timed like its benchmark: steady
+    clock around each step() (benchmark/pbf_benchmark.cu:121-137)."""
+    from oracle import oracle as O
+    from oracle import build_ref
+    if not build_ref.available():
+        return {"unavailable": "reference kernels not built (oracle/_ref needs the reference "
+                               "sources at build time)"}
+    pos, vel, mn, mx, prm, col = scene
+    r = O.RefCudaSolver()
+    r.initialize(len(pos), mn, mx, prm.as_dict())
+    sp = [(*c, rr) for c, rr in col.get("spheres", [])]
+    bx = [(*c, *e) for c, e in col.get("boxes", [])]
+    r.set_colliders(np.asarray(sp, np.float32).reshape(-1, 4),
+                    np.asarray(bx, np.float32).reshape(-1, 6), np.zeros((0, 6), np.float32))
+    r.set_particles(pos, vel)
+    st = r.run(warmup)
+    if st != 0:
+        return {"unavailable": "reference step failed with status %d" % st}
+    ms = r.time_steps(steps)
+    r.close()
+    return {"value": len(pos) * steps / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms / steps,
+            "steps": steps, "warmup": warmup,
+            "method": "reference kernels compiled from its sources (-O3 -DNDEBUG, sm_103a), "
+                      "PBFSolver host sequence and synchronisation, steady_clock around each "
+                      "step()"}
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
@@ -259,6 +288,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--scene", default="dam_break_1m")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-cuda", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--max-neighbors", type=int, default=256,
                     help="neighbour list capacity (the reference fixes 256)")
@@ -381,6 +411,10 @@ def main():
             "stages": stages,
             "density_error": {"mean": density[0], "max": density[1]},
         }
+        if world == 1 and not args.no_reference_cuda:
+            line["reference_cuda"] = reference_cuda(scene, min(args.steps, 50), args.warmup)
+            if "value" in line["reference_cuda"]:
+                line["speedup_vs_reference_cuda"] = value / line["reference_cuda"]["value"]
         if not args.no_cpu_baseline and world == 1:
             budget = float(os.environ.get("PBF_CPU_SECONDS", "20"))
             line["cpu_baseline"] = cpu_baseline(scene, seconds_budget=budget)
