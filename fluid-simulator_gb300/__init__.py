@@ -180,6 +180,8 @@ def _declare(L):
         "pbf_resolve_velocities": ([_vp, _vp, _vp, sz, F3, F3, _vp, sz, _vp, sz, _vp, sz, fl, fl,
                                     fl], S),
         "pbf_integrate": ([_vp, _vp, _vp, sz, fl, F3], S),
+        "pbf_grid_build_static_scratch": ([_vp, sz, F3, F3, fl, _vp, _vp, _vp, _vp, _vp], S),
+        "pbf_static_scratch_capacity": ([], sz),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)

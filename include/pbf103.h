@@ -219,6 +219,28 @@ pbf_status pbf_resolve_velocities(const pbf_float4* positions,
                                   const pbf_plane* planes, size_t plane_count,
                                   float particle_radius, float restitution, float friction);
 
+/* Grid build that allocates no device memory.  No counterpart in the
+ * reference: it is for callers that must not allocate while they run --
+ * latency-bound or real-time loops, where cudaMalloc/cudaFree can block or
+ * synchronise the whole device, and programs whose device memory belongs to a
+ * pool or framework allocator that does not allow raw cudaMalloc beside it.
+ * Same results as pbf_grid_build, but every array is a caller-owned DEVICE
+ * array (num_cells = dims product entries for cell_start/cell_end) and the
+ * work is enqueued on `stream` (a cudaStream_t, NULL = default stream)
+ * without waiting for it.  Its working memory is one fixed array inside the
+ * library, pbf_static_scratch_capacity() particles large (262,144), which every
+ * GPU that loads the library keeps until the process exits; larger counts are
+ * rejected with PBF_ERR_LENGTH.  The first call on a device looks up that
+ * array's device address (make it before any stream capture).  All calls share
+ * the array: calls whose GPU work overlaps in time race and must be ordered
+ * by the caller (for example by issuing them on one stream). */
+pbf_status pbf_grid_build_static_scratch(const pbf_float4* d_positions, size_t count,
+                                         pbf_float3 min_bounds, pbf_float3 max_bounds,
+                                         float cell_size, uint32_t* d_sorted_keys,
+                                         uint32_t* d_sorted_indices, int* d_cell_start,
+                                         int* d_cell_end, void* stream);
+size_t pbf_static_scratch_capacity(void);
+
 /* integrate (src/pbf/integration.cu:6-32) in place on host arrays. */
 pbf_status pbf_integrate(const pbf_float4* positions, pbf_float4* predicted,
                          pbf_float4* velocities, size_t count, float dt, pbf_float3 gravity);
