@@ -26,8 +26,10 @@
 #include <utility>
 #include <vector>
 
-namespace {
-
+// Parameter and container layouts of the reference (SimulationParams,
+// Container).  Kept outside the anonymous namespace: the extern "C" entry
+// points take them, and a parameter type with internal linkage would give
+// those functions internal linkage too.
 struct RefParams {  // SimulationParams layout
     float dt, restDensity, particleMass, particleRadius, collisionRestitution, collisionFriction,
         smoothingRadius, lambdaEpsilon;
@@ -40,6 +42,8 @@ struct RefParams {  // SimulationParams layout
 struct RefContainer {
     float3 min, max;
 };
+
+namespace {
 
 constexpr int kBlock = 256;
 constexpr int kMaxNeighbors = 256;
