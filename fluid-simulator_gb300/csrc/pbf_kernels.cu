@@ -86,12 +86,17 @@ k_cell_first(const uint32_t* __restrict__ skeys, int n, uint32_t cells, int* __r
 __global__ void __launch_bounds__(kBlock)
 k_gather_xs(const uint32_t* __restrict__ perm, const float4* __restrict__ xs_in,
             float4* __restrict__ xs_out, const uint32_t* __restrict__ org_in,
-            uint32_t* __restrict__ org_out, int n, const unsigned* __restrict__ status) {
+            uint32_t* __restrict__ org_out, float* __restrict__ sx, float* __restrict__ sy,
+            float* __restrict__ sz, int n, const unsigned* __restrict__ status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || fatal(status)) return;
     const uint32_t p = perm[i];
-    xs_out[i] = xs_in[p];
-    org_out[i] = org_in ? org_in[p] : p;
+    const float4 q = xs_in[p];
+    xs_out[i] = q;
+    sx[i] = q.x;
+    sy[i] = q.y;
+    sz[i] = q.z;
+    if (org_out) org_out[i] = org_in ? org_in[p] : p;
 }
 
 // ---------------------------------------------------------------------------
@@ -123,11 +128,22 @@ __device__ __forceinline__ float lambda_finish(const StepConst& c, const LambdaA
     return fdiv(-C, denom);
 }
 
+// One candidate of the walk: the same test and append as the reference's
+// inner loop (neighbors.cu:329-350).
+__device__ __forceinline__ void take(float d2, float h2, int j, int i, int max_nb,
+                                     uint32_t* __restrict__ out, size_t stride, int& count) {
+    if (d2 <= h2 && j != i) {
+        if (count < max_nb) out[static_cast<size_t>(count) * stride] = static_cast<uint32_t>(j);
+        ++count;
+    }
+}
+
 template <bool LAMBDA>
 __global__ void __launch_bounds__(kBlock)
-k_search(const float4* __restrict__ xs, const int* __restrict__ first, StepConst c, int n,
-         uint32_t* __restrict__ nbr, int* __restrict__ cnt, float* __restrict__ lam,
-         unsigned* __restrict__ status) {
+k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
+         const float* __restrict__ sy, const float* __restrict__ sz, const int* __restrict__ first,
+         StepConst c, int n, uint32_t* __restrict__ nbr, int* __restrict__ cnt,
+         float* __restrict__ lam, unsigned* __restrict__ status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || fatal(status)) return;
     const float4 pi = xs[i];
@@ -142,33 +158,51 @@ k_search(const float4* __restrict__ xs, const int* __restrict__ first, StepConst
     const uint32_t gx = static_cast<uint32_t>(c.g.gx);
     const uint32_t gxy = gx * static_cast<uint32_t>(c.g.gy);
     const float h2 = c.k.h2;
+    const int max_nb = c.max_nb;
     uint32_t* __restrict__ out = nbr + i;
     const size_t stride = c.stride;
+    const f32x2 px = pack2(pi.x, pi.x), py = pack2(pi.y, pi.y), pz = pack2(pi.z, pi.z);
     int count = 0;
     // Rows z -> y; inside a row the cells x0..x1 are consecutive keys, so the
     // candidates of the row are one index range walked in ascending order --
     // exactly the reference's z -> y -> x cell walk (neighbors.cu:319-354).
+    // Candidates are tested two at a time with FP32x2 arithmetic on the
+    // component arrays (8-byte pair loads); a leading odd index and a
+    // trailing single candidate use the scalar path.
     for (int z = z0; z <= z1; ++z) {
         for (int y = y0; y <= y1; ++y) {
             const uint32_t row = static_cast<uint32_t>(y) * gx + static_cast<uint32_t>(z) * gxy;
-            const int s = __ldg(&first[row + static_cast<uint32_t>(x0)]);
+            int j = __ldg(&first[row + static_cast<uint32_t>(x0)]);
             const int e = __ldg(&first[row + static_cast<uint32_t>(x1) + 1u]);
-#pragma unroll 4
-            for (int j = s; j < e; ++j) {
-                const float4 pj = __ldg(&xs[j]);
-                const float d2 = dist2(fsub(pi.x, pj.x), fsub(pi.y, pj.y), fsub(pi.z, pj.z));
-                if (d2 <= h2 && j != i) {
-                    if (count < c.max_nb) out[static_cast<size_t>(count) * stride] =
-                        static_cast<uint32_t>(j);
-                    ++count;
-                }
+            if ((j & 1) && j < e) {
+                const float d2 = dist2(fsub(pi.x, __ldg(&sx[j])), fsub(pi.y, __ldg(&sy[j])),
+                                       fsub(pi.z, __ldg(&sz[j])));
+                take(d2, h2, j, i, max_nb, out, stride, count);
+                ++j;
+            }
+#pragma unroll 2
+            for (; j + 2 <= e; j += 2) {
+                const float2 X = __ldg(reinterpret_cast<const float2*>(sx + j));
+                const float2 Y = __ldg(reinterpret_cast<const float2*>(sy + j));
+                const float2 Z = __ldg(reinterpret_cast<const float2*>(sz + j));
+                const f32x2 d2 = dist2x2(sub2(px, pack2(X.x, X.y)), sub2(py, pack2(Y.x, Y.y)),
+                                         sub2(pz, pack2(Z.x, Z.y)));
+                float da, db;
+                unpack2(d2, da, db);
+                take(da, h2, j, i, max_nb, out, stride, count);
+                take(db, h2, j + 1, i, max_nb, out, stride, count);
+            }
+            if (j < e) {
+                const float d2 = dist2(fsub(pi.x, __ldg(&sx[j])), fsub(pi.y, __ldg(&sy[j])),
+                                       fsub(pi.z, __ldg(&sz[j])));
+                take(d2, h2, j, i, max_nb, out, stride, count);
             }
         }
     }
     cnt[i] = count;
-    if (count > c.max_nb) atomicOr(status, kStatusNeighborOverflow);
+    if (count > max_nb) atomicOr(status, kStatusNeighborOverflow);
     if (LAMBDA) {
-        if (count > c.max_nb) {
+        if (count > max_nb) {
             lam[i] = CUDART_NAN_F;
             return;
         }
@@ -220,18 +254,20 @@ struct PosLam {
 // computeDeltaPosition summed in list order (pbf_solver_kernels.cu:134-171).
 // Indices, positions and lambdas of four neighbours are loaded before any of
 // them is used, so the dependent gathers overlap; the sum stays in list order.
+template <int N>
 __device__ __forceinline__ void delta_term(const StepConst& c, float4 pi, float li, float4 pj,
                                            float lj, float& ax, float& ay, float& az) {
     const float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y), dz = fsub(pi.z, pj.z);
     const float d2 = dist2(dx, dy, dz);
     float gx, gy, gz;
     spiky(c.k, dx, dy, dz, d2, gx, gy, gz);
-    const float ls = fadd(fadd(li, lj), scorr(c.sc, d2));
+    const float ls = fadd(fadd(li, lj), scorr<N>(c.sc, d2));
     ax = ffma(ls, gx, ax);
     ay = ffma(ls, gy, ay);
     az = ffma(ls, gz, az);
 }
 
+template <int N>
 __device__ __forceinline__ void delta_sum(const StepConst& c, const float4* __restrict__ xs,
                                           const uint32_t* __restrict__ nbr,
                                           const float* __restrict__ lam, int i, int count,
@@ -241,13 +277,15 @@ __device__ __forceinline__ void delta_sum(const StepConst& c, const float4* __re
     for_each_neighbor<4, PosLam>(
         nbr + i, c.stride, count,
         [&](uint32_t j) { return PosLam{__ldg(&xs[j]), __ldg(&lam[j])}; },
-        [&](const PosLam& q) { delta_term(c, pi, li, q.p, q.l, ax, ay, az); });
+        [&](const PosLam& q) { delta_term<N>(c, pi, li, q.p, q.l, ax, ay, az); });
     dpx = fmul(c.gs, ax);
     dpy = fmul(c.gs, ay);
     dpz = fmul(c.gs, az);
 }
 
 // delta p + applyDeltaPosition + CollisionSystem::solve + next cell keys.
+// N: artificial-pressure exponent fixed at compile time (0 = read at run time).
+template <int N>
 __global__ void __launch_bounds__(kBlock)
 k_delta_apply(const float4* __restrict__ xs, const uint32_t* __restrict__ nbr,
               const int* __restrict__ cnt, const float* __restrict__ lam, StepConst c, int n,
@@ -261,7 +299,7 @@ k_delta_apply(const float4* __restrict__ xs, const uint32_t* __restrict__ nbr,
     if (!count_ok(count, c.max_nb)) {
         dpx = dpy = dpz = CUDART_NAN_F;
     } else {
-        delta_sum(c, xs, nbr, lam, i, count, pi, dpx, dpy, dpz);
+        delta_sum<N>(c, xs, nbr, lam, i, count, pi, dpx, dpy, dpz);
     }
     float px = fadd(pi.x, dpx), py = fadd(pi.y, dpy), pz = fadd(pi.z, dpz);
     if (!project_all(c.col, c.particle_radius, px, py, pz))
@@ -488,7 +526,7 @@ k_delta_list(const float4* __restrict__ xs, const uint32_t* __restrict__ nbr,
         return;
     }
     float dx, dy, dz;
-    delta_sum(c, xs, nbr, lam, i, count, xs[i], dx, dy, dz);
+    delta_sum<0>(c, xs, nbr, lam, i, count, xs[i], dx, dy, dz);
     delta[i] = make_float4(dx, dy, dz, 0.0f);
 }
 
@@ -541,22 +579,32 @@ void launch_cell_first(const uint32_t* skeys, int n, uint64_t cells, int* first,
                                                            first, status);
 }
 void launch_gather_xs(const uint32_t* perm, const float4* xs_in, float4* xs_out,
-                      const uint32_t* org_in, uint32_t* org_out, int n, const unsigned* status,
-                      cudaStream_t st) {
-    k_gather_xs<<<blocks_for(n), kBlock, 0, st>>>(perm, xs_in, xs_out, org_in, org_out, n, status);
+                      const uint32_t* org_in, uint32_t* org_out, float* sx, float* sy, float* sz,
+                      int n, const unsigned* status, cudaStream_t st) {
+    k_gather_xs<<<blocks_for(n), kBlock, 0, st>>>(perm, xs_in, xs_out, org_in, org_out, sx, sy, sz,
+                                                  n, status);
 }
-void launch_search(const float4* xs, const int* first, const StepConst& c, int n, uint32_t* nbr,
-                   int* cnt, float* lam, unsigned* status, bool with_lambda, cudaStream_t st) {
+void launch_search(const float4* xs, const float* sx, const float* sy, const float* sz,
+                   const int* first, const StepConst& c, int n, uint32_t* nbr, int* cnt, float* lam,
+                   unsigned* status, bool with_lambda, cudaStream_t st) {
     if (with_lambda)
-        k_search<true><<<blocks_for(n), kBlock, 0, st>>>(xs, first, c, n, nbr, cnt, lam, status);
+        k_search<true><<<blocks_for(n), kBlock, 0, st>>>(xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
+                                                         status);
     else
-        k_search<false><<<blocks_for(n), kBlock, 0, st>>>(xs, first, c, n, nbr, cnt, lam, status);
+        k_search<false><<<blocks_for(n), kBlock, 0, st>>>(xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
+                                                          status);
 }
 void launch_delta_apply(const float4* xs, const uint32_t* nbr, const int* cnt, const float* lam,
                         const StepConst& c, int n, float4* xs_out, uint32_t* keys_out,
                         unsigned* status, cudaStream_t st) {
-    k_delta_apply<<<blocks_for(n), kBlock, 0, st>>>(xs, nbr, cnt, lam, c, n, xs_out, keys_out,
-                                                    status);
+    const unsigned g = blocks_for(n);
+    switch (c.sc.k != 0.0f ? c.sc.n : 0) {
+        case 1: k_delta_apply<1><<<g, kBlock, 0, st>>>(xs, nbr, cnt, lam, c, n, xs_out, keys_out, status); break;
+        case 2: k_delta_apply<2><<<g, kBlock, 0, st>>>(xs, nbr, cnt, lam, c, n, xs_out, keys_out, status); break;
+        case 3: k_delta_apply<3><<<g, kBlock, 0, st>>>(xs, nbr, cnt, lam, c, n, xs_out, keys_out, status); break;
+        case 4: k_delta_apply<4><<<g, kBlock, 0, st>>>(xs, nbr, cnt, lam, c, n, xs_out, keys_out, status); break;
+        default: k_delta_apply<0><<<g, kBlock, 0, st>>>(xs, nbr, cnt, lam, c, n, xs_out, keys_out, status); break;
+    }
 }
 void launch_finalize(const uint32_t* org, const float4* x_old, const float4* vin_old,
                      const float4* v_old, const uint32_t* id_old, const float4* xs, int n,

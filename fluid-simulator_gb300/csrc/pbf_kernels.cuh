@@ -36,14 +36,17 @@ void launch_predict(const float4* x, const float4* v, float4* xs, float4* vin, u
                     int n, const StepConst& c, const unsigned* status, cudaStream_t st);
 void launch_cell_ranges(const uint32_t* skeys, int* cell_start, int* cell_end, int n,
                         const unsigned* status, cudaStream_t st);
+// Reorders predicted positions (float4 and x/y/z component arrays for the
+// search) and composes the substep permutation; org_out may be null.
 void launch_gather_xs(const uint32_t* perm, const float4* xs_in, float4* xs_out,
-                      const uint32_t* org_in, uint32_t* org_out, int n, const unsigned* status,
-                      cudaStream_t st);
+                      const uint32_t* org_in, uint32_t* org_out, float* sx, float* sy, float* sz,
+                      int n, const unsigned* status, cudaStream_t st);
 // first: lower bound of every cell key, cells + 1 entries (launch_cell_first).
 void launch_cell_first(const uint32_t* skeys, int n, uint64_t cells, int* first,
                        const unsigned* status, cudaStream_t st);
-void launch_search(const float4* xs, const int* first, const StepConst& c, int n, uint32_t* nbr,
-                   int* cnt, float* lam, unsigned* status, bool with_lambda, cudaStream_t st);
+void launch_search(const float4* xs, const float* sx, const float* sy, const float* sz,
+                   const int* first, const StepConst& c, int n, uint32_t* nbr, int* cnt, float* lam,
+                   unsigned* status, bool with_lambda, cudaStream_t st);
 void launch_delta_apply(const float4* xs, const uint32_t* nbr, const int* cnt, const float* lam,
                         const StepConst& c, int n, float4* xs_out, uint32_t* keys_out,
                         unsigned* status, cudaStream_t st);

@@ -35,12 +35,45 @@ __device__ __forceinline__ float ffma(float a, float b, float c) { return __fmaf
 __device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ float fsqrt(float a) { return __fsqrt_rn(a); }
 
-// Squared length, fused as the compiled reference expression
-// dx*dx + dy*dy + dz*dz (src/pbf/neighbors.cu:338-342).
+// Packed pair of floats for the FP32x2 instructions of sm_100+: each lane is
+// rounded exactly like the scalar add/mul/fma.rn, so pairs give the same bits.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pack2(float a, float b) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void unpack2(f32x2 r, float& a, float& b) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+    return r;
+}
+
+// Squared length, rounded as the reference's compiled findNeighbors rounds
+// dx*dx + dy*dy + dz*dz (src/pbf/neighbors.cu:338-342): nvcc contracts it to
+// fma(dz, dz, fma(dy, dy, dx*dx)).  Neighbour lists can only match the
+// reference bit for bit with this exact rounding.
 __device__ __forceinline__ float dist2(float dx, float dy, float dz) {
-    return ffma(dz, dz, ffma(dx, dx, fmul(dy, dy)));
+    return ffma(dz, dz, ffma(dy, dy, fmul(dx, dx)));
 }
 __device__ __forceinline__ float len3(float x, float y, float z) { return fsqrt(dist2(x, y, z)); }
+// dist2 of two displacements at once (lane-wise identical to dist2).
+__device__ __forceinline__ f32x2 dist2x2(f32x2 dx, f32x2 dy, f32x2 dz) {
+    return fma2(dz, dz, fma2(dy, dy, mul2(dx, dx)));
+}
 // a.y*b.z - a.z*b.y with one rounding of the first product.
 __device__ __forceinline__ float crossc(float ay, float az, float by, float bz) {
     return ffma(ay, bz, -fmul(az, by));
@@ -117,12 +150,28 @@ __device__ __forceinline__ float ipow(float b, int n) {
     return r;
 }
 
+// ipow with the exponent known at compile time: the same products in the
+// same order as the loop above (b^2, b^4 = (b^2)^2, 1 * x == x exactly).
+template <int N>
+__device__ __forceinline__ float ipow_c(float b) {
+    if (N == 1) return b;
+    if (N == 2) return fmul(b, b);
+    if (N == 3) return fmul(b, fmul(b, b));
+    if (N == 4) {
+        const float b2 = fmul(b, b);
+        return fmul(b2, b2);
+    }
+    return ipow(b, N);
+}
+
+// N > 0: exponent fixed at compile time; N == 0: exponent read from s.n.
+template <int N = 0>
 __device__ __forceinline__ float scorr(const ScorrConst& s, float d2) {
     if (s.k == 0.0f || s.n <= 0) return 0.0f;
     if (d2 >= s.h2 || s.dq2 >= s.h2) return 0.0f;
     const float ratio = fmul(fsub(s.h2, d2), s.inv_den);
     const float r3 = fmul(fmul(ratio, ratio), ratio);
-    return fmul(s.negk, ipow(r3, s.n));
+    return fmul(s.negk, N > 0 ? ipow_c<N>(r3) : ipow(r3, s.n));
 }
 
 // Grid geometry: cell = floor((p - min) / cellSize) per axis with an IEEE

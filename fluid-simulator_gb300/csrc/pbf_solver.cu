@@ -154,6 +154,10 @@ struct pbf_solver {
     DeviceBuffer ids[2], org[2];
     DeviceBuffer keys, skeys, sidx, akeys, aidx;
     DeviceBuffer cell_first, nbr, cnt, lam, sort_scratch, status, tmp4, ftmp;
+    DeviceBuffer soa;  // x, y, z components of the reordered predicted positions
+    // Component array stride: a multiple of 64 floats, so every array starts
+    // 256-byte aligned and the search's even-index pair loads are 8-byte aligned.
+    size_t soa_stride() const { return (cap + 63) / 64 * 64; }
     unsigned* h_status = nullptr;
     int ix = 0, iv = 1, iid = 0;  // roles: positions, velocities, ids
 
@@ -295,7 +299,9 @@ struct pbf_solver {
                 M(kStGather);
                 launch_gather_xs(sidx.as<uint32_t>(), P(cur), P(nxt),
                                  org_cur < 0 ? nullptr : org[org_cur].as<uint32_t>(),
-                                 org[org_next].as<uint32_t>(), N, sp, st);
+                                 org[org_next].as<uint32_t>(), soa.as<float>(),
+                                 soa.as<float>() + soa_stride(), soa.as<float>() + 2 * soa_stride(), N, sp,
+                                 st);
                 give(cur);
                 cur = nxt;
                 org_cur = org_next;
@@ -303,8 +309,9 @@ struct pbf_solver {
             for (int it = 0; it < prm.solverIterations; ++it) {
                 rebuild();
                 M(kStSearchLambda);
-                launch_search(P(cur), cell_first.as<int>(), c, N, nbr.as<uint32_t>(),
-                              cnt.as<int>(), lam.as<float>(), sp, true, st);
+                launch_search(P(cur), soa.as<float>(), soa.as<float>() + soa_stride(),
+                              soa.as<float>() + 2 * soa_stride(), cell_first.as<int>(), c, N,
+                              nbr.as<uint32_t>(), cnt.as<int>(), lam.as<float>(), sp, true, st);
                 const int nxt = take();
                 M(kStDeltaApply);
                 launch_delta_apply(P(cur), nbr.as<uint32_t>(), cnt.as<int>(), lam.as<float>(), c,
@@ -315,8 +322,9 @@ struct pbf_solver {
             if (post) {
                 rebuild();
                 M(kStSearch);
-                launch_search(P(cur), cell_first.as<int>(), c, N, nbr.as<uint32_t>(),
-                              cnt.as<int>(), nullptr, sp, false, st);
+                launch_search(P(cur), soa.as<float>(), soa.as<float>() + soa_stride(),
+                              soa.as<float>() + 2 * soa_stride(), cell_first.as<int>(), c, N,
+                              nbr.as<uint32_t>(), cnt.as<int>(), nullptr, sp, false, st);
             }
             const int vnew = take();
             const int vinnew = take();
@@ -494,6 +502,7 @@ struct pbf_solver {
         for (auto& b : norg) b.allocate(u4b);
         DeviceBuffer nkeys(u4b), nskeys(u4b), nsidx(u4b), nakeys(u4b), naidx(u4b);
         DeviceBuffer nfirst((ncells + 1) * sizeof(int));
+        DeviceBuffer nsoa(3 * ((max_particles + 63) / 64 * 64) * sizeof(float));
         DeviceBuffer nnbr(strd * size_t(maxnb) * sizeof(uint32_t));
         DeviceBuffer ncnt(u4b), nlam(u4b), nscr(sort_scratch_bytes(int(max_particles)));
         DeviceBuffer nstat(sizeof(unsigned)), ntmp(f4b), nftmp(u4b);
@@ -510,6 +519,7 @@ struct pbf_solver {
         akeys = std::move(nakeys);
         aidx = std::move(naidx);
         cell_first = std::move(nfirst);
+        soa = std::move(nsoa);
         nbr = std::move(nnbr);
         cnt = std::move(ncnt);
         lam = std::move(nlam);

@@ -212,9 +212,19 @@ pbf_status pbf_find_neighbors(const pbf_float4* sorted_positions, size_t count,
         StepConst c = kernel_const(h, 1.0f, 1.0f, max_neighbors, stride);
         c.k.h2 = h * h;
         c.g = grid_const(mn, cell, dims, h);
-        launch_search(dpos.as<float4>(), dfirst.as<int>(), c, static_cast<int>(count),
-                      dnb.as<uint32_t>(), dcnt.as<int>(), nullptr, dstat.as<unsigned>(), false,
-                      nullptr);
+        // Component arrays for the search (identity gather of the given order).
+        // Padded to 64 floats per component so pair loads stay 8-byte aligned.
+        const size_t pad = (count + 63) / 64 * 64;
+        DeviceBuffer dsoa(3 * pad * sizeof(float)), dids(count * sizeof(uint32_t)),
+            dcopy(count * sizeof(float4));
+        launch_iota(dids.as<uint32_t>(), static_cast<int>(count), nullptr);
+        float* sx = dsoa.as<float>();
+        launch_gather_xs(dids.as<uint32_t>(), dpos.as<float4>(), dcopy.as<float4>(), nullptr,
+                         nullptr, sx, sx + pad, sx + 2 * pad, static_cast<int>(count), nullptr,
+                         nullptr);
+        launch_search(dpos.as<float4>(), sx, sx + pad, sx + 2 * pad, dfirst.as<int>(), c,
+                      static_cast<int>(count), dnb.as<uint32_t>(), dcnt.as<int>(), nullptr,
+                      dstat.as<unsigned>(), false, nullptr);
         cuda_check(cudaGetLastError());
         cuda_check(cudaDeviceSynchronize());
         download(neighbors, dnb, list);

@@ -64,9 +64,10 @@ struct F32 {
         c_poly6 = 315.0f / (64.0f * kPiF) / hh / hh / hh;
         c_spiky = -45.0f / kPiF / hh / hh / hh / hh;
     }
-    // Squared length; the fused pattern matches the compiled reference
-    // expression dx*dx + dy*dy + dz*dz (src/pbf/neighbors.cu:338-342).
-    static T dist2(T dx, T dy, T dz) { return std::fma(dz, dz, std::fma(dx, dx, dy * dy)); }
+    // Squared length rounded as the reference's compiled findNeighbors rounds
+    // dx*dx + dy*dy + dz*dz (src/pbf/neighbors.cu:338-342): fma(dz, dz,
+    // fma(dy, dy, dx*dx)).
+    static T dist2(T dx, T dy, T dz) { return std::fma(dz, dz, std::fma(dy, dy, dx * dx)); }
     static T len(T x, T y, T z) { return std::sqrt(dist2(x, y, z)); }
     // poly6FromDistanceSquared (include/pbf/sph_helpers.cuh:13-34).
     T poly6(T d2) const {

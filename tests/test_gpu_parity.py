@@ -119,6 +119,41 @@ def test_grid_build_bit_exact_at_1m(pbf, scenes):
     np.testing.assert_array_equal(got[3], ends)
 
 
+def test_distance_rounding_on_contraction_pairs(pbf):
+    """Pairs whose decision depends on the rounding of d2 (golden fixture):
+    the CUDA search decides exactly like the reference's findNeighbors."""
+    import os
+    f = np.load(os.path.join(os.path.dirname(__file__), "golden", "contraction_pairs.npz"))
+    pos, dec = f["positions"], f["decisions"][:, [str(x) for x in f["forms"]].index("z(y(xx))")]
+    mn, mx, h = (0.0, 0.0, 0.0), (20.0, 20.0, 20.0), 0.1
+    sk, si, cs, ce = pbf.grid_build(pos, mn, mx, h)
+    nb, cnt, ov = pbf.find_neighbors(pos[si], cs, ce, pbf.grid_dims(mn, mx, h), mn, h, h, 8,
+                                     len(pos))
+    counts = np.zeros(len(pos), np.int32)
+    counts[si] = cnt
+    np.testing.assert_array_equal(counts[0::2].astype(bool), dec)
+    np.testing.assert_array_equal(counts[1::2].astype(bool), dec)
+
+
+def test_substeps_equal_repeated_single_steps(pbf, scenes):
+    """A frame of S substeps is S steps of dt/S (src/pbf/pbf_solver.cu:193-198):
+    bit-identical positions and velocities."""
+    pos, vel, mn, mx, prm, col = scenes.reference_benchmark(8192)
+    p2 = prm.as_dict()
+    p1 = dict(p2, substeps=1, dt=float(np.float32(p2["dt"]) / np.float32(p2["substeps"])))
+    out = []
+    for p, frames in ((p2, 3), (p1, 3 * p2["substeps"])):
+        s = pbf.PBFSolver()
+        s.initialize(len(pos), mn, mx, pbf.SimulationParams(**p))
+        s.set_spheres(col["spheres"])
+        s.set_boxes(col["boxes"])
+        s.set_particles(pos, vel)
+        s.run(frames)
+        out.append((s.copy_positions_to_host(), s.copy_velocities_to_host()))
+    assert_bitwise(out[0][0], out[1][0], "positions")
+    assert_bitwise(out[0][1], out[1][1], "velocities")
+
+
 def test_neighbor_lists_bit_exact_vs_oracle_slot_order(pbf, scenes, orc):
     """Slot-major lists in walk order, identical to the oracle's findNeighbors."""
     pos, _, mn, mx, prm, _ = scenes.dam_break_16k()
