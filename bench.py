@@ -41,8 +41,9 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s at 1M (4 iters)"
 UNIT = "particle-steps/s"
 WORKLOAD = ("dam_break_1m: 1,048,576 particles (128x128x64 lattice, spacing 0.5h, jitter "
-            "+-0.01h seed 0) in a 12.8x6.4x6.4 box, h=0.1, rho0=6378, dt=1/60, 1 substep, "
-            "4 iterations, scorr k=0.1 n=4 dq=0.2h, eps=600, xsph 0.01, vorticity 1e-4")
+            "+-0.01h seed 0) in a 12.8x6.4x6.4 box, h=0.1, rho0=6378, dt=1/120 per step, "
+            "1 substep, 4 iterations, scorr k=1e-4 n=4 dq=0.2h, eps=600, xsph 1e-5, "
+            "vorticity 1e-5, friction 0.03, 256 neighbour slots")
 # Algorithmic bytes per particle-step: 492 + I*(128 + 8C) + 8C with I = 4
 # iterations and C = cells/particle (minimal compulsory traffic: integrate,
 # hash, counting sort, reorder, lambda, delta-p + apply, final rebuild, the
@@ -412,7 +413,7 @@ def main():
             "density_error": {"mean": density[0], "max": density[1]},
         }
         if world == 1 and not args.no_reference_cuda:
-            line["reference_cuda"] = reference_cuda(scene, min(args.steps, 50), args.warmup)
+            line["reference_cuda"] = reference_cuda(scene, args.steps, args.warmup)
             if "value" in line["reference_cuda"]:
                 line["speedup_vs_reference_cuda"] = value / line["reference_cuda"]["value"]
         if not args.no_cpu_baseline and world == 1:

@@ -128,16 +128,6 @@ __device__ __forceinline__ float lambda_finish(const StepConst& c, const LambdaA
     return fdiv(-C, denom);
 }
 
-// One candidate of the walk: the same test and append as the reference's
-// inner loop (neighbors.cu:329-350).
-__device__ __forceinline__ void take(float d2, float h2, int j, int i, int max_nb,
-                                     uint32_t* __restrict__ out, size_t stride, int& count) {
-    if (d2 <= h2 && j != i) {
-        if (count < max_nb) out[static_cast<size_t>(count) * stride] = static_cast<uint32_t>(j);
-        ++count;
-    }
-}
-
 template <bool LAMBDA>
 __global__ void __launch_bounds__(kBlock)
 k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
@@ -166,36 +156,46 @@ k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
     // Rows z -> y; inside a row the cells x0..x1 are consecutive keys, so the
     // candidates of the row are one index range walked in ascending order --
     // exactly the reference's z -> y -> x cell walk (neighbors.cu:319-354).
-    // Candidates are tested two at a time with FP32x2 arithmetic on the
-    // component arrays (8-byte pair loads); a leading odd index and a
-    // trailing single candidate use the scalar path.
+    // Each range is scanned in 32-candidate chunks starting at an even index:
+    // pairs of candidates are tested with FP32x2 arithmetic on the component
+    // arrays (8-byte loads), the results go into a hit mask without branches,
+    // and the hits are then appended in ascending order.  Candidates outside
+    // [s, e) and the particle itself are masked off; the component arrays
+    // are padded so the odd element past e is always readable.
     for (int z = z0; z <= z1; ++z) {
         for (int y = y0; y <= y1; ++y) {
             const uint32_t row = static_cast<uint32_t>(y) * gx + static_cast<uint32_t>(z) * gxy;
-            int j = __ldg(&first[row + static_cast<uint32_t>(x0)]);
+            const int s = __ldg(&first[row + static_cast<uint32_t>(x0)]);
             const int e = __ldg(&first[row + static_cast<uint32_t>(x1) + 1u]);
-            if ((j & 1) && j < e) {
-                const float d2 = dist2(fsub(pi.x, __ldg(&sx[j])), fsub(pi.y, __ldg(&sy[j])),
-                                       fsub(pi.z, __ldg(&sz[j])));
-                take(d2, h2, j, i, max_nb, out, stride, count);
-                ++j;
-            }
-#pragma unroll 2
-            for (; j + 2 <= e; j += 2) {
-                const float2 X = __ldg(reinterpret_cast<const float2*>(sx + j));
-                const float2 Y = __ldg(reinterpret_cast<const float2*>(sy + j));
-                const float2 Z = __ldg(reinterpret_cast<const float2*>(sz + j));
-                const f32x2 d2 = dist2x2(sub2(px, pack2(X.x, X.y)), sub2(py, pack2(Y.x, Y.y)),
-                                         sub2(pz, pack2(Z.x, Z.y)));
-                float da, db;
-                unpack2(d2, da, db);
-                take(da, h2, j, i, max_nb, out, stride, count);
-                take(db, h2, j + 1, i, max_nb, out, stride, count);
-            }
-            if (j < e) {
-                const float d2 = dist2(fsub(pi.x, __ldg(&sx[j])), fsub(pi.y, __ldg(&sy[j])),
-                                       fsub(pi.z, __ldg(&sz[j])));
-                take(d2, h2, j, i, max_nb, out, stride, count);
+            for (int j0 = s & ~1; j0 < e; j0 += 32) {
+                const int lim = min(32, e - j0);
+                uint32_t mask = 0u;
+#pragma unroll 4
+                for (int b = 0; b < lim; b += 2) {
+                    const float2 X = __ldg(reinterpret_cast<const float2*>(sx + j0 + b));
+                    const float2 Y = __ldg(reinterpret_cast<const float2*>(sy + j0 + b));
+                    const float2 Z = __ldg(reinterpret_cast<const float2*>(sz + j0 + b));
+                    const f32x2 d2 = dist2x2(sub2(px, pack2(X.x, X.y)),
+                                             sub2(py, pack2(Y.x, Y.y)),
+                                             sub2(pz, pack2(Z.x, Z.y)));
+                    float da, db;
+                    unpack2(d2, da, db);
+                    mask |= (static_cast<uint32_t>(da <= h2) |
+                             (static_cast<uint32_t>(db <= h2) << 1)) << b;
+                }
+                // Keep bits of [s, e) only, and drop the particle itself.
+                uint32_t valid = lim >= 32 ? 0xffffffffu : ((1u << lim) - 1u);
+                if (j0 < s) valid &= ~((1u << (s - j0)) - 1u);
+                const int self = i - j0;
+                if (self >= 0 && self < 32) valid &= ~(1u << self);
+                mask &= valid;
+                while (mask) {
+                    const int b = __ffs(mask) - 1;
+                    mask &= mask - 1u;
+                    if (count < max_nb)
+                        out[static_cast<size_t>(count) * stride] = static_cast<uint32_t>(j0 + b);
+                    ++count;
+                }
             }
         }
     }

@@ -156,8 +156,9 @@ struct pbf_solver {
     DeviceBuffer cell_first, nbr, cnt, lam, sort_scratch, status, tmp4, ftmp;
     DeviceBuffer soa;  // x, y, z components of the reordered predicted positions
     // Component array stride: a multiple of 64 floats, so every array starts
-    // 256-byte aligned and the search's even-index pair loads are 8-byte aligned.
-    size_t soa_stride() const { return (cap + 63) / 64 * 64; }
+    // 256-byte aligned and the search's even-index pair loads are 8-byte
+    // aligned; at least cap + 1 so a pair may read one element past the end.
+    size_t soa_stride() const { return (cap + 1 + 63) / 64 * 64; }
     unsigned* h_status = nullptr;
     int ix = 0, iv = 1, iid = 0;  // roles: positions, velocities, ids
 
@@ -502,7 +503,7 @@ struct pbf_solver {
         for (auto& b : norg) b.allocate(u4b);
         DeviceBuffer nkeys(u4b), nskeys(u4b), nsidx(u4b), nakeys(u4b), naidx(u4b);
         DeviceBuffer nfirst((ncells + 1) * sizeof(int));
-        DeviceBuffer nsoa(3 * ((max_particles + 63) / 64 * 64) * sizeof(float));
+        DeviceBuffer nsoa(3 * ((max_particles + 1 + 63) / 64 * 64) * sizeof(float));
         DeviceBuffer nnbr(strd * size_t(maxnb) * sizeof(uint32_t));
         DeviceBuffer ncnt(u4b), nlam(u4b), nscr(sort_scratch_bytes(int(max_particles)));
         DeviceBuffer nstat(sizeof(unsigned)), ntmp(f4b), nftmp(u4b);
