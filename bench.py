@@ -57,7 +57,7 @@ def b_alg(iters: int, cells_per_particle: float) -> float:
 STAGE_BYTES = {
     "predict": 64.0 + 20.0,          # R x, v; W x*, v_in; + hash of the first rebuild
     "sort": 8.0,                      # R key, W permutation
-    "gather": 44.0,                   # R perm, R/W x*, R/W composed permutation
+    "gather_ranges": 46.0,            # R perm, R/W x*, R/W composed permutation, first[]
     "search_lambda": 24.0,            # R x*, W lambda, W count
     "delta_apply_collide": 56.0,      # R x*, R lambda, W x* + next hash
     "search_final": 20.0,

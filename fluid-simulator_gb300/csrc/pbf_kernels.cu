@@ -3,8 +3,9 @@
 // Hot path per constraint iteration (reference: src/pbf/pbf_solver.cu:210-258):
 //   k_predict        integrate + v_in copy + first cell keys      (integration.cu:6-32)
 //   [sort]           stable radix sort of (key, index)            (spatial_grid.cu:188-196)
-//   k_cell_ranges    half-open [start, end) per occupied cell     (spatial_grid.cu:123-137)
-//   k_gather_xs      reorder predicted positions + compose the permutation
+//   k_gather_first   reorder predicted positions, compose the permutation and
+//                    refresh first[] (lower bound of every cell key; the row
+//                    walk's form of cellStart/cellEnd, spatial_grid.cu:123-137)
 //   k_search<true>   neighbour walk + lambda in one pass           (neighbors.cu:3-91,
 //                                                                  pbf_solver_kernels.cu:26-105)
 //   k_delta_apply    delta p + apply + collision projection + next keys
@@ -20,9 +21,15 @@
 // pbf_math.cuh so the host oracle reproduces the step bit for bit.
 #include "pbf_kernels.cuh"
 
+#include "pbf_common.h"
+
 #include <math_constants.h>
 
+#include <algorithm>
+
 namespace pbf {
+
+void launch_error_check(cudaError_t e) { cuda_check(e); }
 
 namespace {
 
@@ -70,20 +77,6 @@ k_cell_ranges(const uint32_t* __restrict__ skeys, int* __restrict__ cs, int* __r
 // cells resolved to the next occupied one, so a run of cells along x is one
 // contiguous index range.
 __global__ void __launch_bounds__(kBlock)
-k_cell_first(const uint32_t* __restrict__ skeys, int n, uint32_t cells, int* __restrict__ first,
-             const unsigned* __restrict__ status) {
-    const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k > cells || fatal(status)) return;
-    int lo = 0, hi = n;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (__ldg(&skeys[mid]) < k) lo = mid + 1;
-        else hi = mid;
-    }
-    first[k] = lo;
-}
-
-__global__ void __launch_bounds__(kBlock)
 k_gather_xs(const uint32_t* __restrict__ perm, const float4* __restrict__ xs_in,
             float4* __restrict__ xs_out, const uint32_t* __restrict__ org_in,
             uint32_t* __restrict__ org_out, float* __restrict__ sx, float* __restrict__ sy,
@@ -97,6 +90,71 @@ k_gather_xs(const uint32_t* __restrict__ perm, const float4* __restrict__ xs_in,
     sy[i] = q.y;
     sz[i] = q.z;
     if (org_out) org_out[i] = org_in ? org_in[p] : p;
+}
+
+// Lower bound of key k in skeys[0, n), searched outward from a guess: the
+// table of the previous rebuild, whose entries move little between
+// iterations.  Any guess gives the same answer; a good one needs one or two
+// loads instead of log2(n).
+__device__ __forceinline__ int lower_bound_from(const uint32_t* __restrict__ skeys, int n,
+                                                uint32_t k, int guess) {
+    int g = min(max(guess, 0), n);
+    int lo, hi;  // answer in [lo, hi]
+    if (g > 0 && __ldg(&skeys[g - 1]) >= k) {
+        // Answer < g: gallop down until skeys[lo - 1] < k (or lo == 0).
+        hi = g - 1;
+        int step = 1;
+        lo = g - 1;
+        while (lo > 0 && __ldg(&skeys[lo - 1]) >= k) {
+            hi = lo - 1;
+            lo = lo > step ? lo - step : 0;
+            step = step < (1 << 29) ? step << 1 : step;
+        }
+    } else if (g < n && __ldg(&skeys[g]) < k) {
+        // Answer > g: gallop up until skeys[hi] >= k (or hi == n).
+        lo = g + 1;
+        int step = 1;
+        hi = min(n, g + 1);
+        while (hi < n && __ldg(&skeys[hi]) < k) {
+            lo = hi + 1;
+            hi = n - hi > step ? hi + step : n;
+            step = step < (1 << 29) ? step << 1 : step;
+        }
+    } else {
+        return g;
+    }
+    // Invariant: skeys[lo - 1] < k (or lo == 0) and skeys[hi] >= k (or hi == n).
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(&skeys[mid]) < k) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// One launch after each sort: thread i reorders particle i (as k_gather_xs)
+// and refreshes first[i] for i <= cells, in place.
+__global__ void __launch_bounds__(kBlock)
+k_gather_first(const uint32_t* __restrict__ perm, const float4* __restrict__ xs_in,
+               float4* __restrict__ xs_out, const uint32_t* __restrict__ org_in,
+               uint32_t* __restrict__ org_out, float* __restrict__ sx, float* __restrict__ sy,
+               float* __restrict__ sz, int n, const uint32_t* __restrict__ skeys, uint32_t cells,
+               int* __restrict__ first, const unsigned* __restrict__ status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (fatal(status)) return;
+    if (i < n) {
+        const uint32_t p = perm[i];
+        const float4 q = xs_in[p];
+        xs_out[i] = q;
+        sx[i] = q.x;
+        sy[i] = q.y;
+        sz[i] = q.z;
+        org_out[i] = org_in ? org_in[p] : p;
+    }
+    if (static_cast<uint32_t>(i) <= cells) {
+        const uint32_t k = static_cast<uint32_t>(i);
+        first[k] = lower_bound_from(skeys, n, k, first[k]);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -567,16 +625,11 @@ k_integrate(const float4* __restrict__ x, float4* __restrict__ xs, float4* __res
 // --- launchers ---------------------------------------------------------------
 void launch_predict(const float4* x, const float4* v, float4* xs, float4* vin, uint32_t* keys,
                     int n, const StepConst& c, const unsigned* status, cudaStream_t st) {
-    k_predict<<<blocks_for(n), kBlock, 0, st>>>(x, v, xs, vin, keys, n, c, status);
+    launch_k(k_predict, blocks_for(n), kBlock, st, x, v, xs, vin, keys, n, c, status);
 }
 void launch_cell_ranges(const uint32_t* skeys, int* cs, int* ce, int n, const unsigned* status,
                         cudaStream_t st) {
     k_cell_ranges<<<blocks_for(n), kBlock, 0, st>>>(skeys, cs, ce, n, status);
-}
-void launch_cell_first(const uint32_t* skeys, int n, uint64_t cells, int* first,
-                       const unsigned* status, cudaStream_t st) {
-    k_cell_first<<<blocks_for(cells + 1), kBlock, 0, st>>>(skeys, n, static_cast<uint32_t>(cells),
-                                                           first, status);
 }
 void launch_gather_xs(const uint32_t* perm, const float4* xs_in, float4* xs_out,
                       const uint32_t* org_in, uint32_t* org_out, float* sx, float* sy, float* sz,
@@ -584,14 +637,22 @@ void launch_gather_xs(const uint32_t* perm, const float4* xs_in, float4* xs_out,
     k_gather_xs<<<blocks_for(n), kBlock, 0, st>>>(perm, xs_in, xs_out, org_in, org_out, sx, sy, sz,
                                                   n, status);
 }
+void launch_gather_first(const uint32_t* perm, const float4* xs_in, float4* xs_out,
+                         const uint32_t* org_in, uint32_t* org_out, float* sx, float* sy, float* sz,
+                         int n, const uint32_t* skeys, uint64_t cells, int* first,
+                         const unsigned* status, cudaStream_t st) {
+    const uint64_t threads = std::max<uint64_t>(static_cast<uint64_t>(n), cells + 1);
+    launch_k(k_gather_first, blocks_for(threads), kBlock, st, perm, xs_in, xs_out, org_in, org_out,
+             sx, sy, sz, n, skeys, static_cast<uint32_t>(cells), first, status);
+}
 void launch_search(const float4* xs, const float* sx, const float* sy, const float* sz,
                    const int* first, const StepConst& c, int n, uint32_t* nbr, int* cnt, float* lam,
                    unsigned* status, bool with_lambda, cudaStream_t st) {
     if (with_lambda)
-        k_search<true><<<blocks_for(n), kBlock, 0, st>>>(xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
+        launch_k(k_search<true>, blocks_for(n), kBlock, st, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
                                                          status);
     else
-        k_search<false><<<blocks_for(n), kBlock, 0, st>>>(xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
+        launch_k(k_search<false>, blocks_for(n), kBlock, st, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
                                                           status);
 }
 void launch_delta_apply(const float4* xs, const uint32_t* nbr, const int* cnt, const float* lam,
@@ -599,39 +660,39 @@ void launch_delta_apply(const float4* xs, const uint32_t* nbr, const int* cnt, c
                         unsigned* status, cudaStream_t st) {
     const unsigned g = blocks_for(n);
     switch (c.sc.k != 0.0f ? c.sc.n : 0) {
-        case 1: k_delta_apply<1><<<g, kBlock, 0, st>>>(xs, nbr, cnt, lam, c, n, xs_out, keys_out, status); break;
-        case 2: k_delta_apply<2><<<g, kBlock, 0, st>>>(xs, nbr, cnt, lam, c, n, xs_out, keys_out, status); break;
-        case 3: k_delta_apply<3><<<g, kBlock, 0, st>>>(xs, nbr, cnt, lam, c, n, xs_out, keys_out, status); break;
-        case 4: k_delta_apply<4><<<g, kBlock, 0, st>>>(xs, nbr, cnt, lam, c, n, xs_out, keys_out, status); break;
-        default: k_delta_apply<0><<<g, kBlock, 0, st>>>(xs, nbr, cnt, lam, c, n, xs_out, keys_out, status); break;
+        case 1: launch_k(k_delta_apply<1>, g, kBlock, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out, status); break;
+        case 2: launch_k(k_delta_apply<2>, g, kBlock, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out, status); break;
+        case 3: launch_k(k_delta_apply<3>, g, kBlock, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out, status); break;
+        case 4: launch_k(k_delta_apply<4>, g, kBlock, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out, status); break;
+        default: launch_k(k_delta_apply<0>, g, kBlock, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out, status); break;
     }
 }
 void launch_finalize(const uint32_t* org, const float4* x_old, const float4* vin_old,
                      const float4* v_old, const uint32_t* id_old, const float4* xs, int n,
                      const StepConst& c, float4* v_new, float4* vin_new, uint32_t* id_new,
                      const unsigned* status, cudaStream_t st) {
-    k_finalize<<<blocks_for(n), kBlock, 0, st>>>(org, x_old, vin_old, v_old, id_old, xs, n, c,
+    launch_k(k_finalize, blocks_for(n), kBlock, st, org, x_old, vin_old, v_old, id_old, xs, n, c,
                                                  v_new, vin_new, id_new, status);
 }
 void launch_xsph(const float4* x, const float4* v, const uint32_t* nbr, const int* cnt,
                  const StepConst& c, int n, float4* v_out, const float4* vin, bool resolve,
                  const unsigned* status, cudaStream_t st) {
-    k_xsph<<<blocks_for(n), kBlock, 0, st>>>(x, v, nbr, cnt, c, n, v_out, vin, resolve, status);
+    launch_k(k_xsph, blocks_for(n), kBlock, st, x, v, nbr, cnt, c, n, v_out, vin, resolve, status);
 }
 void launch_vorticity(const float4* x, const float4* v, const uint32_t* nbr, const int* cnt,
                       const StepConst& c, int n, float4* omega, const unsigned* status,
                       cudaStream_t st) {
-    k_vorticity<<<blocks_for(n), kBlock, 0, st>>>(x, v, nbr, cnt, c, n, omega, status);
+    launch_k(k_vorticity, blocks_for(n), kBlock, st, x, v, nbr, cnt, c, n, omega, status);
 }
 void launch_confine(const float4* x, const uint32_t* nbr, const int* cnt, const float4* omega,
                     const float4* v, const StepConst& c, int n, float4* v_out,
                     const float4* vin, bool resolve, const unsigned* status, cudaStream_t st) {
-    k_confine<<<blocks_for(n), kBlock, 0, st>>>(x, nbr, cnt, omega, v, c, n, v_out, vin, resolve,
+    launch_k(k_confine, blocks_for(n), kBlock, st, x, nbr, cnt, omega, v, c, n, v_out, vin, resolve,
                                                 status);
 }
 void launch_resolve(const float4* x, const float4* vin, float4* v, const StepConst& c, int n,
                     const unsigned* status, cudaStream_t st) {
-    k_resolve<<<blocks_for(n), kBlock, 0, st>>>(x, vin, v, c, n, status);
+    launch_k(k_resolve, blocks_for(n), kBlock, st, x, vin, v, c, n, status);
 }
 void launch_scatter_by_id(const float4* vals, const uint32_t* id, float4* out, int n,
                           cudaStream_t st) {

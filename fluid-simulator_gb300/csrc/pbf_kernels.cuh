@@ -31,6 +31,21 @@ inline unsigned blocks_for(size_t n, int block = kBlock) {
     return static_cast<unsigned>((n + block - 1) / block);
 }
 
+// Launches kernel k on stream st; launch errors throw like cuda_check.
+void launch_error_check(cudaError_t e);
+template <typename... P, typename... A>
+inline void launch_k(void (*k)(P...), unsigned grid, unsigned block, cudaStream_t st, A&&... a) {
+    if (grid == 0) return;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cfg.attrs = nullptr;
+    cfg.numAttrs = 0;
+    launch_error_check(cudaLaunchKernelEx(&cfg, k, static_cast<P>(a)...));
+}
+
 // --- step kernels (pbf_kernels.cu) -----------------------------------------
 void launch_predict(const float4* x, const float4* v, float4* xs, float4* vin, uint32_t* keys,
                     int n, const StepConst& c, const unsigned* status, cudaStream_t st);
@@ -41,9 +56,13 @@ void launch_cell_ranges(const uint32_t* skeys, int* cell_start, int* cell_end, i
 void launch_gather_xs(const uint32_t* perm, const float4* xs_in, float4* xs_out,
                       const uint32_t* org_in, uint32_t* org_out, float* sx, float* sy, float* sz,
                       int n, const unsigned* status, cudaStream_t st);
-// first: lower bound of every cell key, cells + 1 entries (launch_cell_first).
-void launch_cell_first(const uint32_t* skeys, int n, uint64_t cells, int* first,
-                       const unsigned* status, cudaStream_t st);
+// launch_gather_xs with org_out set, fused with the refresh of first[]
+// (lower bound of every cell key, cells + 1 entries), which is updated in
+// place: its previous contents only seed the search.
+void launch_gather_first(const uint32_t* perm, const float4* xs_in, float4* xs_out,
+                         const uint32_t* org_in, uint32_t* org_out, float* sx, float* sy, float* sz,
+                         int n, const uint32_t* skeys, uint64_t cells, int* first,
+                         const unsigned* status, cudaStream_t st);
 void launch_search(const float4* xs, const float* sx, const float* sy, const float* sz,
                    const int* first, const StepConst& c, int n, uint32_t* nbr, int* cnt, float* lam,
                    unsigned* status, bool with_lambda, cudaStream_t st);

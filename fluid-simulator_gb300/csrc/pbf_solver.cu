@@ -52,11 +52,11 @@ constexpr int kF4Pool = 6;                 // float4 buffers rotated through rol
 
 // Stages of one frame, for the event profiler (pbf_profile_frame).
 enum Stage {
-    kStPredict, kStSort, kStRanges, kStGather, kStSearchLambda, kStDeltaApply, kStSearch,
+    kStPredict, kStSort, kStGatherRanges, kStSearchLambda, kStDeltaApply, kStSearch,
     kStFinalize, kStXsph, kStVorticity, kStConfine, kStResolve, kStageCount
 };
 const char* const kStageNames[kStageCount] = {
-    "predict", "sort", "cell_ranges", "gather", "search_lambda", "delta_apply_collide",
+    "predict", "sort", "gather_ranges", "search_lambda", "delta_apply_collide",
     "search_final", "finalize", "xsph", "vorticity", "confine_resolve", "resolve"};
 
 // Event marks recorded between the launches of a frame; interval i belongs to
@@ -293,16 +293,15 @@ struct pbf_solver {
                 M(kStSort);
                 launch_sort(plan, keys.as<uint32_t>(), skeys.as<uint32_t>(), sidx.as<uint32_t>(),
                             akeys.as<uint32_t>(), aidx.as<uint32_t>(), sort_scratch.get(), sp, st);
-                M(kStRanges);
-                launch_cell_first(skeys.as<uint32_t>(), N, cells, cell_first.as<int>(), sp, st);
                 const int nxt = take();
                 const int org_next = org_cur < 0 ? 0 : 1 - org_cur;
-                M(kStGather);
-                launch_gather_xs(sidx.as<uint32_t>(), P(cur), P(nxt),
-                                 org_cur < 0 ? nullptr : org[org_cur].as<uint32_t>(),
-                                 org[org_next].as<uint32_t>(), soa.as<float>(),
-                                 soa.as<float>() + soa_stride(), soa.as<float>() + 2 * soa_stride(), N, sp,
-                                 st);
+                M(kStGatherRanges);
+                launch_gather_first(sidx.as<uint32_t>(), P(cur), P(nxt),
+                                    org_cur < 0 ? nullptr : org[org_cur].as<uint32_t>(),
+                                    org[org_next].as<uint32_t>(), soa.as<float>(),
+                                    soa.as<float>() + soa_stride(),
+                                    soa.as<float>() + 2 * soa_stride(), N, skeys.as<uint32_t>(),
+                                    cells, cell_first.as<int>(), sp, st);
                 give(cur);
                 cur = nxt;
                 org_cur = org_next;

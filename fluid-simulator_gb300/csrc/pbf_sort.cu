@@ -4,10 +4,12 @@
 // (src/pbf/spatial_grid.cu:188-196).  A stable sort has one result whatever
 // the digit schedule, so only the bits that can be non-zero are sorted:
 // keys are clamped cell ids < num_cells.  Each pass is reduce-then-scan:
-//   upsweep   per-tile digit histogram (shared-memory atomics) + digit totals
-//   scan      one block per digit: exclusive scan over tiles + digit base
-//   downsweep stable in-tile ranks (warp match + per-warp running counters,
-//             items visited in index order) and scatter
+//   upsweep   per-tile digit histogram (shared-memory atomics)
+//   scan      one block per digit: exclusive scan over tiles + digit total
+//   downsweep digit bases from the totals, stable in-tile ranks (warp match
+//             + per-warp running counters, items visited in index order),
+//             tile staged in shared memory in digit order, then written out
+//             as contiguous runs (coalesced stores)
 // No kernel waits on another block, so nothing can spin.
 #include "pbf_kernels.cuh"
 
@@ -17,12 +19,13 @@ namespace pbf {
 
 namespace {
 
-constexpr int kSortThreads = 256;
+constexpr int kSortThreads = 512;
 constexpr int kSortWarps = kSortThreads / 32;
-constexpr int kSortItems = 16;                         // per thread
+constexpr int kSortItems = 8;                          // per thread
 constexpr int kTile = kSortThreads * kSortItems;       // 4096 keys per tile
-constexpr int kWarpChunk = kTile / kSortWarps;         // 512 consecutive keys per warp
+constexpr int kWarpChunk = kTile / kSortWarps;         // 256 consecutive keys per warp
 constexpr int kMaxBins = 256;
+static_assert(kMaxBins <= kSortThreads, "one digit per thread in the prologues");
 
 __device__ __forceinline__ bool fatal(const unsigned* status) {
     return status != nullptr && (__ldcg(status) & kStatusFatalMask) != 0u;
@@ -30,8 +33,7 @@ __device__ __forceinline__ bool fatal(const unsigned* status) {
 
 __global__ void __launch_bounds__(kSortThreads)
 k_upsweep(const uint32_t* __restrict__ keys, int n, int shift, uint32_t mask, int tiles,
-          uint32_t* __restrict__ hist, uint32_t* __restrict__ totals,
-          const unsigned* __restrict__ status) {
+          uint32_t* __restrict__ hist, const unsigned* __restrict__ status) {
     if (fatal(status)) return;
     __shared__ uint32_t cnt[kMaxBins];
     const int bins = static_cast<int>(mask) + 1;
@@ -42,14 +44,11 @@ k_upsweep(const uint32_t* __restrict__ keys, int n, int shift, uint32_t mask, in
     for (int i = base + threadIdx.x; i < end; i += kSortThreads)
         atomicAdd(&cnt[(keys[i] >> shift) & mask], 1u);
     __syncthreads();
-    for (int d = threadIdx.x; d < bins; d += kSortThreads) {
-        const uint32_t c = cnt[d];
-        hist[static_cast<size_t>(d) * tiles + blockIdx.x] = c;
-        if (c) atomicAdd(&totals[d], c);
-    }
+    for (int d = threadIdx.x; d < bins; d += kSortThreads)
+        hist[static_cast<size_t>(d) * tiles + blockIdx.x] = cnt[d];
 }
 
-// Block-wide exclusive scan helper over kSortThreads values.
+// Block-wide exclusive scan over kSortThreads values.
 __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* smem_warp,
                                                          uint32_t& total) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -77,19 +76,14 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s
     return warp_base + incl - v;
 }
 
-// One block per digit: offsets[d][t] = base(d) + sum_{t' < t} hist[d][t'].
+// One block per digit: hist[d][t] <- sum_{t' < t} hist[d][t'], totals[d] <- row sum.
 __global__ void __launch_bounds__(kSortThreads)
-k_scan(uint32_t* __restrict__ hist, const uint32_t* __restrict__ totals, int tiles,
+k_scan(uint32_t* __restrict__ hist, uint32_t* __restrict__ totals, int tiles,
        const unsigned* __restrict__ status) {
     if (fatal(status)) return;
     __shared__ uint32_t warp_sums[kSortWarps];
     const int d = blockIdx.x;
-    // Digit base: sum of the totals of all smaller digits.
-    uint32_t part = 0;
-    for (int e = threadIdx.x; e < d; e += kSortThreads) part += totals[e];
-    uint32_t base_total;
-    (void)block_exclusive_scan(part, warp_sums, base_total);
-    uint32_t running = base_total;
+    uint32_t running = 0;
     uint32_t* row = hist + static_cast<size_t>(d) * tiles;
     for (int t0 = 0; t0 < tiles; t0 += kSortThreads) {
         const int t = t0 + threadIdx.x;
@@ -99,38 +93,62 @@ k_scan(uint32_t* __restrict__ hist, const uint32_t* __restrict__ totals, int til
         if (t < tiles) row[t] = running + ex;
         running += chunk_total;
     }
+    if (threadIdx.x == 0) totals[d] = running;
 }
 
 __global__ void __launch_bounds__(kSortThreads)
 k_downsweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
             uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, int n, int shift,
             uint32_t mask, int tiles, const uint32_t* __restrict__ offsets,
-            const unsigned* __restrict__ status) {
+            const uint32_t* __restrict__ totals, const unsigned* __restrict__ status) {
     if (fatal(status)) return;
-    __shared__ uint32_t wcnt[kSortWarps][kMaxBins];
-    __shared__ uint32_t tile_off[kMaxBins];
+    // The per-warp digit counters are dead once every item holds its
+    // in-tile position, so the staging area for the tile reuses them.
+    constexpr int kCountWords = kSortWarps * kMaxBins;
+    constexpr int kStageWords = 2 * kTile;
+    __shared__ uint32_t pool[kCountWords > kStageWords ? kCountWords : kStageWords];
+    __shared__ uint32_t tile_off[kMaxBins];    // global start of each digit's run
+    __shared__ uint32_t tile_start[kMaxBins];  // in-tile start of each digit
+    __shared__ uint32_t warp_sums[kSortWarps];
+    uint32_t(*wcnt)[kMaxBins] = reinterpret_cast<uint32_t(*)[kMaxBins]>(pool);
+    uint32_t* skey = pool;
+    uint32_t* sval = pool + kTile;
+
     const int bins = static_cast<int>(mask) + 1;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (int d = threadIdx.x; d < bins; d += kSortThreads) {
-        tile_off[d] = offsets[static_cast<size_t>(d) * tiles + blockIdx.x];
+    const int tid = threadIdx.x;
+    const int lane = tid & 31, warp = tid >> 5;
+    const int tile_base = blockIdx.x * kTile;
+    const int base = tile_base + warp * kWarpChunk;
+    uint32_t k_reg[kSortItems], v_reg[kSortItems], r_reg[kSortItems];
+    // All loads of the warp's chunk are issued first; their latency overlaps
+    // the prologue.
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        const int idx = base + r * 32 + lane;
+        k_reg[r] = idx < n ? keys_in[idx] : 0u;
+        v_reg[r] = idx < n ? (vals_in ? vals_in[idx] : static_cast<uint32_t>(idx)) : 0u;
+    }
+    for (int d = tid; d < bins; d += kSortThreads) {
 #pragma unroll
         for (int w = 0; w < kSortWarps; ++w) wcnt[w][d] = 0;
+    }
+    // Digit bases: exclusive scan of the digit totals.
+    {
+        const uint32_t tot = tid < bins ? totals[tid] : 0u;
+        uint32_t all;
+        const uint32_t dbase = block_exclusive_scan(tot, warp_sums, all);
+        if (tid < bins)
+            tile_off[tid] = dbase + offsets[static_cast<size_t>(tid) * tiles + blockIdx.x];
     }
     __syncthreads();
 
     const uint32_t lt_mask = (1u << lane) - 1u;
-    const int base = blockIdx.x * kTile + warp * kWarpChunk;
-    uint32_t k_reg[kSortItems], v_reg[kSortItems], r_reg[kSortItems];
 #pragma unroll
     for (int r = 0; r < kSortItems; ++r) {
         const int idx = base + r * 32 + lane;
         const bool valid = idx < n;
-        uint32_t key = 0, val = 0, digit = 0xffffffffu;
-        if (valid) {
-            key = keys_in[idx];
-            val = vals_in ? vals_in[idx] : static_cast<uint32_t>(idx);
-            digit = (key >> shift) & mask;
-        }
+        const uint32_t key = k_reg[r];
+        const uint32_t digit = valid ? (key >> shift) & mask : 0xffffffffu;
         const uint32_t peers = __match_any_sync(0xffffffffu, digit);
         const int leader = __ffs(peers) - 1;
         uint32_t prior = 0;
@@ -139,30 +157,50 @@ k_downsweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ v
             wcnt[warp][digit] = prior + __popc(peers);
         }
         prior = __shfl_sync(0xffffffffu, prior, leader);
-        k_reg[r] = key;
-        v_reg[r] = val;
         r_reg[r] = valid ? prior + __popc(peers & lt_mask) : 0xffffffffu;
         __syncwarp();
     }
     __syncthreads();
-    // Exclusive scan over the warps of each digit: earlier warps hold earlier keys.
-    for (int d = threadIdx.x; d < bins; d += kSortThreads) {
-        uint32_t run = 0;
+    // Exclusive scan over the warps of each digit (earlier warps hold
+    // earlier keys), then over the digits of the tile.
+    uint32_t dcount = 0;
+    if (tid < bins) {
 #pragma unroll
         for (int w = 0; w < kSortWarps; ++w) {
-            const uint32_t c = wcnt[w][d];
-            wcnt[w][d] = run;
-            run += c;
+            const uint32_t c = wcnt[w][tid];
+            wcnt[w][tid] = dcount;
+            dcount += c;
         }
+    }
+    {
+        uint32_t all;
+        const uint32_t start = block_exclusive_scan(dcount, warp_sums, all);
+        if (tid < bins) tile_start[tid] = start;
     }
     __syncthreads();
 #pragma unroll
     for (int r = 0; r < kSortItems; ++r) {
         if (r_reg[r] == 0xffffffffu) continue;
         const uint32_t digit = (k_reg[r] >> shift) & mask;
-        const uint32_t dst = tile_off[digit] + wcnt[warp][digit] + r_reg[r];
-        keys_out[dst] = k_reg[r];
-        vals_out[dst] = v_reg[r];
+        r_reg[r] += tile_start[digit] + wcnt[warp][digit];
+    }
+    __syncthreads();  // every counter read before the staging area overwrites them
+#pragma unroll
+    for (int r = 0; r < kSortItems; ++r) {
+        if (r_reg[r] == 0xffffffffu) continue;
+        skey[r_reg[r]] = k_reg[r];
+        sval[r_reg[r]] = v_reg[r];
+    }
+    __syncthreads();
+    // Staged tile in digit order: consecutive threads write consecutive
+    // positions of each digit's run.
+    const int count = min(kTile, n - tile_base);
+    for (int k = tid; k < count; k += kSortThreads) {
+        const uint32_t key = skey[k];
+        const uint32_t digit = (key >> shift) & mask;
+        const uint32_t dst = tile_off[digit] + (static_cast<uint32_t>(k) - tile_start[digit]);
+        keys_out[dst] = key;
+        vals_out[dst] = sval[k];
     }
 }
 
@@ -201,12 +239,11 @@ void launch_sort(const SortPlan& plan, const uint32_t* keys, uint32_t* sorted_ke
         uint32_t* kout = to_sorted ? sorted_keys : alt_keys;
         uint32_t* vout = to_sorted ? sorted_idx : alt_idx;
         const int shift = p * plan.bits_per_pass;
-        cudaMemsetAsync(totals, 0, kMaxBins * sizeof(uint32_t), st);
-        k_upsweep<<<plan.tiles, kSortThreads, 0, st>>>(kin, plan.n, shift, mask, plan.tiles, hist,
-                                                       totals, status);
-        k_scan<<<plan.bins, kSortThreads, 0, st>>>(hist, totals, plan.tiles, status);
-        k_downsweep<<<plan.tiles, kSortThreads, 0, st>>>(kin, vin, kout, vout, plan.n, shift, mask,
-                                                         plan.tiles, hist, status);
+        launch_k(k_upsweep, plan.tiles, kSortThreads, st, kin, plan.n, shift, mask, plan.tiles,
+                 hist, status);
+        launch_k(k_scan, plan.bins, kSortThreads, st, hist, totals, plan.tiles, status);
+        launch_k(k_downsweep, plan.tiles, kSortThreads, st, kin, vin, kout, vout, plan.n, shift,
+                 mask, plan.tiles, hist, totals, status);
         kin = kout;
         vin = vout;
     }
