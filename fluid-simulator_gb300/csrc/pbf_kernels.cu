@@ -178,6 +178,23 @@ __device__ __forceinline__ void lambda_add(const KernelConst& k, LambdaAcc& a, f
     a.gz = fadd(a.gz, gz);
 }
 
+// Two neighbours' terms, lane 0 first: the same sums as two lambda_add calls.
+__device__ __forceinline__ void lambda_add2(const KernelConst& k, LambdaAcc& a, f32x2 dx, f32x2 dy,
+                                            f32x2 dz, f32x2 d2) {
+    const f32x2 s = spiky_scale2(k, d2);
+    float w0, w1, x0, x1, y0, y1, z0, z1;
+    unpack2(poly6_2(k, d2), w0, w1);
+    unpack2(mul2(dx, s), x0, x1);
+    unpack2(mul2(dy, s), y0, y1);
+    unpack2(mul2(dz, s), z0, z1);
+    a.wsum = fadd(fadd(a.wsum, w0), w1);
+    a.s2 = ffma(z0, z0, ffma(y0, y0, ffma(x0, x0, a.s2)));
+    a.s2 = ffma(z1, z1, ffma(y1, y1, ffma(x1, x1, a.s2)));
+    a.gx = fadd(fadd(a.gx, x0), x1);
+    a.gy = fadd(fadd(a.gy, y0), y1);
+    a.gz = fadd(fadd(a.gz, z0), z1);
+}
+
 __device__ __forceinline__ float lambda_finish(const StepConst& c, const LambdaAcc& a) {
     const float rho = fmul(c.mass, a.wsum);
     const float g2 = dist2(a.gx, a.gy, a.gz);
@@ -267,8 +284,20 @@ k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
         // Second pass over the list just written: the constraint terms run
         // once per neighbour instead of once per candidate in which any lane
         // of the warp hit.  Same order as the list, so the same sums.
+        // Neighbours are taken two at a time with FP32x2 arithmetic; the sums
+        // stay in list order.
         LambdaAcc acc{c.k.c_poly6, 0.0f, 0.0f, 0.0f, 0.0f};
-        for (int k = 0; k < count; ++k) {
+        int k = 0;
+#pragma unroll 2
+        for (; k + 2 <= count; k += 2) {
+            const float4 a = __ldg(&xs[out[static_cast<size_t>(k) * stride]]);
+            const float4 b = __ldg(&xs[out[static_cast<size_t>(k + 1) * stride]]);
+            const f32x2 dx = sub2(px, pack2(a.x, b.x));
+            const f32x2 dy = sub2(py, pack2(a.y, b.y));
+            const f32x2 dz = sub2(pz, pack2(a.z, b.z));
+            lambda_add2(c.k, acc, dx, dy, dz, dist2x2(dx, dy, dz));
+        }
+        if (k < count) {
             const float4 pj = __ldg(&xs[out[static_cast<size_t>(k) * stride]]);
             const float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y), dz = fsub(pi.z, pj.z);
             lambda_add(c.k, acc, dx, dy, dz, dist2(dx, dy, dz));
@@ -281,24 +310,33 @@ __device__ __forceinline__ bool count_ok(int count, int max_nb) {
     return count >= 0 && count <= max_nb;
 }
 
-// Walks a slot-major list in order, B neighbours at a time: the B indices,
-// then the B gathers (load(j)), are issued before any use(), so dependent
-// loads overlap while every use() still runs in list order.
-template <int B, class T, class Load, class Use>
-__device__ __forceinline__ void for_each_neighbor(const uint32_t* __restrict__ row, size_t stride,
-                                                  int count, Load load, Use use) {
+// Walks a slot-major list in order: four indices, then the four gathers
+// (load(j)), are issued before any term is used, so dependent loads overlap.
+// Terms are handed over two at a time (use2(first, second)) for FP32x2
+// evaluation; a last odd neighbour goes to use1.  List order is kept.
+template <class T, class Load, class Use2, class Use1>
+__device__ __forceinline__ void for_each_neighbor_pair(const uint32_t* __restrict__ row,
+                                                       size_t stride, int count, Load load,
+                                                       Use2 use2, Use1 use1) {
     int k = 0;
-    for (; k + B <= count; k += B) {
-        uint32_t j[B];
-        T v[B];
+    for (; k + 4 <= count; k += 4) {
+        uint32_t j[4];
+        T v[4];
 #pragma unroll
-        for (int b = 0; b < B; ++b) j[b] = __ldg(&row[static_cast<size_t>(k + b) * stride]);
+        for (int b = 0; b < 4; ++b) j[b] = __ldg(&row[static_cast<size_t>(k + b) * stride]);
 #pragma unroll
-        for (int b = 0; b < B; ++b) v[b] = load(j[b]);
-#pragma unroll
-        for (int b = 0; b < B; ++b) use(v[b]);
+        for (int b = 0; b < 4; ++b) v[b] = load(j[b]);
+        use2(v[0], v[1]);
+        use2(v[2], v[3]);
     }
-    for (; k < count; ++k) use(load(__ldg(&row[static_cast<size_t>(k) * stride])));
+    if (k + 2 <= count) {
+        const uint32_t j0 = __ldg(&row[static_cast<size_t>(k) * stride]);
+        const uint32_t j1 = __ldg(&row[static_cast<size_t>(k + 1) * stride]);
+        const T a = load(j0), b = load(j1);
+        use2(a, b);
+        k += 2;
+    }
+    if (k < count) use1(load(__ldg(&row[static_cast<size_t>(k) * stride])));
 }
 
 struct PosVel {
@@ -308,6 +346,18 @@ struct PosLam {
     float4 p;
     float l;
 };
+
+// Differences a - (b0, b1) of one float against a pair.
+__device__ __forceinline__ f32x2 diff2(float a, float b0, float b1) {
+    return sub2(splat2(a), pack2(b0, b1));
+}
+__device__ __forceinline__ f32x2 rdiff2(float b0, float b1, float a) {
+    return sub2(pack2(b0, b1), splat2(a));
+}
+// crossc on pairs: a.y*b.z - a.z*b.y with one rounding of a.y*b.z.
+__device__ __forceinline__ f32x2 crossc2(f32x2 ay, f32x2 az, f32x2 by, f32x2 bz) {
+    return fma2(ay, bz, mul2(mul2(az, splat2(-1.0f)), by));
+}
 
 // computeDeltaPosition summed in list order (pbf_solver_kernels.cu:134-171).
 // Indices, positions and lambdas of four neighbours are loaded before any of
@@ -325,6 +375,27 @@ __device__ __forceinline__ void delta_term(const StepConst& c, float4 pi, float 
     az = ffma(ls, gz, az);
 }
 
+// Two neighbours' terms, lane 0 first: the same sums as two delta_term calls.
+template <int N>
+__device__ __forceinline__ void delta_term2(const StepConst& c, float4 pi, float li, float4 pa,
+                                            float la, float4 pb, float lb, float& ax, float& ay,
+                                            float& az) {
+    const f32x2 dx = sub2(splat2(pi.x), pack2(pa.x, pb.x));
+    const f32x2 dy = sub2(splat2(pi.y), pack2(pa.y, pb.y));
+    const f32x2 dz = sub2(splat2(pi.z), pack2(pa.z, pb.z));
+    const f32x2 d2 = dist2x2(dx, dy, dz);
+    const f32x2 s = spiky_scale2(c.k, d2);
+    const f32x2 ls = add2(add2(splat2(li), pack2(la, lb)), scorr2<N>(c.sc, d2));
+    float l0, l1, x0, x1, y0, y1, z0, z1;
+    unpack2(ls, l0, l1);
+    unpack2(mul2(dx, s), x0, x1);
+    unpack2(mul2(dy, s), y0, y1);
+    unpack2(mul2(dz, s), z0, z1);
+    ax = ffma(l1, x1, ffma(l0, x0, ax));
+    ay = ffma(l1, y1, ffma(l0, y0, ay));
+    az = ffma(l1, z1, ffma(l0, z0, az));
+}
+
 template <int N>
 __device__ __forceinline__ void delta_sum(const StepConst& c, const float4* __restrict__ xs,
                                           const uint32_t* __restrict__ nbr,
@@ -332,9 +403,12 @@ __device__ __forceinline__ void delta_sum(const StepConst& c, const float4* __re
                                           float4 pi, float& dpx, float& dpy, float& dpz) {
     const float li = lam[i];
     float ax = 0.0f, ay = 0.0f, az = 0.0f;
-    for_each_neighbor<4, PosLam>(
+    for_each_neighbor_pair<PosLam>(
         nbr + i, c.stride, count,
         [&](uint32_t j) { return PosLam{__ldg(&xs[j]), __ldg(&lam[j])}; },
+        [&](const PosLam& a, const PosLam& b) {
+            delta_term2<N>(c, pi, li, a.p, a.l, b.p, b.l, ax, ay, az);
+        },
         [&](const PosLam& q) { delta_term<N>(c, pi, li, q.p, q.l, ax, ay, az); });
     dpx = fmul(c.gs, ax);
     dpy = fmul(c.gs, ay);
@@ -400,9 +474,21 @@ __device__ __forceinline__ float4 xsph_one(const StepConst& c, const float4* __r
         return make_float4(CUDART_NAN_F, CUDART_NAN_F, CUDART_NAN_F, vi.w);
     const float4 pi = x[i];
     float cx = 0.0f, cy = 0.0f, cz = 0.0f;
-    for_each_neighbor<4, PosVel>(
+    for_each_neighbor_pair<PosVel>(
         nbr + i, c.stride, count,
         [&](uint32_t j) { return PosVel{__ldg(&x[j]), __ldg(&v[j])}; },
+        [&](const PosVel& a, const PosVel& b) {
+            float w0, w1, x0, x1, y0, y1, z0, z1;
+            unpack2(poly6_2(c.k, dist2x2(diff2(pi.x, a.p.x, b.p.x), diff2(pi.y, a.p.y, b.p.y),
+                                         diff2(pi.z, a.p.z, b.p.z))),
+                    w0, w1);
+            unpack2(rdiff2(a.v.x, b.v.x, vi.x), x0, x1);
+            unpack2(rdiff2(a.v.y, b.v.y, vi.y), y0, y1);
+            unpack2(rdiff2(a.v.z, b.v.z, vi.z), z0, z1);
+            cx = ffma(x1, w1, ffma(x0, w0, cx));
+            cy = ffma(y1, w1, ffma(y0, w0, cy));
+            cz = ffma(z1, w1, ffma(z0, w0, cz));
+        },
         [&](const PosVel& q) {
             const float w =
                 poly6(c.k, dist2(fsub(pi.x, q.p.x), fsub(pi.y, q.p.y), fsub(pi.z, q.p.z)));
@@ -431,19 +517,35 @@ k_xsph(const float4* __restrict__ x, const float4* __restrict__ v,
 __global__ void __launch_bounds__(kBlock)
 k_vorticity(const float4* __restrict__ x, const float4* __restrict__ v,
             const uint32_t* __restrict__ nbr, const int* __restrict__ cnt, StepConst c, int n,
-            float4* __restrict__ omega, const unsigned* __restrict__ status) {
+            float4* __restrict__ omega, bool store_norm, const unsigned* __restrict__ status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || fatal(status)) return;
     const int count = cnt[i];
     if (!count_ok(count, c.max_nb)) {
-        omega[i] = make_float4(CUDART_NAN_F, CUDART_NAN_F, CUDART_NAN_F, 0.0f);
+        omega[i] = make_float4(CUDART_NAN_F, CUDART_NAN_F, CUDART_NAN_F,
+                               store_norm ? CUDART_NAN_F : 0.0f);
         return;
     }
     const float4 pi = x[i], vi = v[i];
     float ox = 0.0f, oy = 0.0f, oz = 0.0f;
-    for_each_neighbor<4, PosVel>(
+    for_each_neighbor_pair<PosVel>(
         nbr + i, c.stride, count,
         [&](uint32_t j) { return PosVel{__ldg(&x[j]), __ldg(&v[j])}; },
+        [&](const PosVel& a, const PosVel& b) {
+            const f32x2 dx = diff2(pi.x, a.p.x, b.p.x), dy = diff2(pi.y, a.p.y, b.p.y),
+                        dz = diff2(pi.z, a.p.z, b.p.z);
+            const f32x2 sc = spiky_scale2(c.k, dist2x2(dx, dy, dz));
+            const f32x2 gx = mul2(dx, sc), gy = mul2(dy, sc), gz = mul2(dz, sc);
+            const f32x2 vx = rdiff2(a.v.x, b.v.x, vi.x), vy = rdiff2(a.v.y, b.v.y, vi.y),
+                        vz = rdiff2(a.v.z, b.v.z, vi.z);
+            float x0, x1, y0, y1, z0, z1;
+            unpack2(crossc2(gy, gz, vy, vz), x0, x1);
+            unpack2(crossc2(gz, gx, vz, vx), y0, y1);
+            unpack2(crossc2(gx, gy, vx, vy), z0, z1);
+            ox = fadd(fadd(ox, x0), x1);
+            oy = fadd(fadd(oy, y0), y1);
+            oz = fadd(fadd(oz, z0), z1);
+        },
         [&](const PosVel& q) {
             const float dx = fsub(pi.x, q.p.x), dy = fsub(pi.y, q.p.y), dz = fsub(pi.z, q.p.z);
             float gx, gy, gz;
@@ -453,7 +555,18 @@ k_vorticity(const float4* __restrict__ x, const float4* __restrict__ v,
             oy = fadd(oy, crossc(gz, gx, vz, vx));
             oz = fadd(oz, crossc(gx, gy, vx, vy));
         });
-    omega[i] = make_float4(ox, oy, oz, 0.0f);
+    // With store_norm, w carries |omega| (read by the confinement for every
+    // neighbour); otherwise w = 0 as computeVorticity writes it.
+    omega[i] = make_float4(ox, oy, oz, store_norm ? len3(ox, oy, oz) : 0.0f);
+}
+
+// w <- |omega| for a vorticity array written with w = 0.
+__global__ void __launch_bounds__(kBlock) k_omega_norm(float4* __restrict__ om, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float4 w = om[i];
+    w.w = len3(w.x, w.y, w.z);
+    om[i] = w;
 }
 
 // applyVorticityConfinement (pbf_solver_kernels.cu:317-385).
@@ -465,13 +578,26 @@ __device__ __forceinline__ float4 confine_one(const StepConst& c, const float4* 
     if (!count_ok(count, c.max_nb))
         return make_float4(CUDART_NAN_F, CUDART_NAN_F, CUDART_NAN_F, vi.w);
     const float4 pi = x[i], wi = om[i];
-    const float wil = len3(wi.x, wi.y, wi.z);
+    const float wil = wi.w;  // |omega_i|, stored by k_vorticity
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
-    for_each_neighbor<4, PosVel>(
+    for_each_neighbor_pair<PosVel>(
         nbr + i, c.stride, count,
         [&](uint32_t j) { return PosVel{__ldg(&x[j]), __ldg(&om[j])}; },
+        [&](const PosVel& a, const PosVel& b) {
+            const f32x2 dx = diff2(pi.x, a.p.x, b.p.x), dy = diff2(pi.y, a.p.y, b.p.y),
+                        dz = diff2(pi.z, a.p.z, b.p.z);
+            const f32x2 sc = spiky_scale2(c.k, dist2x2(dx, dy, dz));
+            float m0, m1, x0, x1, y0, y1, z0, z1;
+            unpack2(rdiff2(a.v.w, b.v.w, wil), m0, m1);
+            unpack2(mul2(dx, sc), x0, x1);
+            unpack2(mul2(dy, sc), y0, y1);
+            unpack2(mul2(dz, sc), z0, z1);
+            ex = ffma(m1, x1, ffma(m0, x0, ex));
+            ey = ffma(m1, y1, ffma(m0, y0, ey));
+            ez = ffma(m1, z1, ffma(m0, z0, ez));
+        },
         [&](const PosVel& q) {
-            const float wjl = len3(q.v.x, q.v.y, q.v.z);
+            const float wjl = q.v.w;
             const float dx = fsub(pi.x, q.p.x), dy = fsub(pi.y, q.p.y), dz = fsub(pi.z, q.p.z);
             float gx, gy, gz;
             spiky(c.k, dx, dy, dz, dist2(dx, dy, dz), gx, gy, gz);
@@ -680,15 +806,19 @@ void launch_xsph(const float4* x, const float4* v, const uint32_t* nbr, const in
     launch_k(k_xsph, blocks_for(n), kBlock, st, x, v, nbr, cnt, c, n, v_out, vin, resolve, status);
 }
 void launch_vorticity(const float4* x, const float4* v, const uint32_t* nbr, const int* cnt,
-                      const StepConst& c, int n, float4* omega, const unsigned* status,
-                      cudaStream_t st) {
-    launch_k(k_vorticity, blocks_for(n), kBlock, st, x, v, nbr, cnt, c, n, omega, status);
+                      const StepConst& c, int n, float4* omega, bool store_norm,
+                      const unsigned* status, cudaStream_t st) {
+    launch_k(k_vorticity, blocks_for(n), kBlock, st, x, v, nbr, cnt, c, n, omega, store_norm,
+             status);
+}
+void launch_omega_norm(float4* omega, int n, cudaStream_t st) {
+    launch_k(k_omega_norm, blocks_for(n), kBlock, st, omega, n);
 }
 void launch_confine(const float4* x, const uint32_t* nbr, const int* cnt, const float4* omega,
                     const float4* v, const StepConst& c, int n, float4* v_out,
                     const float4* vin, bool resolve, const unsigned* status, cudaStream_t st) {
-    launch_k(k_confine, blocks_for(n), kBlock, st, x, nbr, cnt, omega, v, c, n, v_out, vin, resolve,
-                                                status);
+    launch_k(k_confine, blocks_for(n), kBlock, st, x, nbr, cnt, omega, v, c, n, v_out, vin,
+             resolve, status);
 }
 void launch_resolve(const float4* x, const float4* vin, float4* v, const StepConst& c, int n,
                     const unsigned* status, cudaStream_t st) {

@@ -76,9 +76,13 @@ void launch_finalize(const uint32_t* org, const float4* x_old, const float4* vin
 void launch_xsph(const float4* x, const float4* v, const uint32_t* nbr, const int* cnt,
                  const StepConst& c, int n, float4* v_out, const float4* vin, bool resolve,
                  const unsigned* status, cudaStream_t st);
+// store_norm: w = |omega| (the form launch_confine reads) instead of 0.
 void launch_vorticity(const float4* x, const float4* v, const uint32_t* nbr, const int* cnt,
-                      const StepConst& c, int n, float4* omega, const unsigned* status,
-                      cudaStream_t st);
+                      const StepConst& c, int n, float4* omega, bool store_norm,
+                      const unsigned* status, cudaStream_t st);
+// Sets w = |omega| in a vorticity array written with w = 0.
+void launch_omega_norm(float4* omega, int n, cudaStream_t st);
+// omega: w = |omega| (launch_vorticity with store_norm, or launch_omega_norm).
 void launch_confine(const float4* x, const uint32_t* nbr, const int* cnt, const float4* omega,
                     const float4* v, const StepConst& c, int n, float4* v_out,
                     const float4* vin, bool resolve, const unsigned* status, cudaStream_t st);

@@ -62,6 +62,13 @@ __device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
     return r;
 }
 
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+    f32x2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+    return r;
+}
+__device__ __forceinline__ f32x2 splat2(float a) { return pack2(a, a); }
+
 // Squared length, rounded as the reference's compiled findNeighbors rounds
 // dx*dx + dy*dy + dz*dz (src/pbf/neighbors.cu:338-342): nvcc contracts it to
 // fma(dz, dz, fma(dy, dy, dx*dx)).  Neighbour lists can only match the
@@ -105,20 +112,84 @@ __device__ __forceinline__ float poly6(const KernelConst& k, float d2) {
     return fmul(k.c_poly6, t3);
 }
 
-// spikyGradientFromDistanceSquared (include/pbf/sph_helpers.cuh:48-81).
+// poly6 of two squared distances (lane-wise identical to poly6).
+__device__ __forceinline__ f32x2 poly6_2(const KernelConst& k, f32x2 d2) {
+    const f32x2 t = fma2(d2, splat2(-k.inv_h2), splat2(1.0f));
+    const f32x2 w = mul2(splat2(k.c_poly6), mul2(mul2(t, t), t));
+    float a, b, da, db;
+    unpack2(w, a, b);
+    unpack2(d2, da, db);
+    if (da >= k.h2) a = 0.0f;
+    if (db >= k.h2) b = 0.0f;
+    return pack2(a, b);
+}
+
+// Reciprocal square root by Newton's method from the bit-level seed of
+// C. Lomont, "Fast Inverse Square Root" (2003), constant 0x5f375a86: three
+// steps y <- y (3/2 - (x/2) y^2), each a correctly rounded multiply or fma,
+// so the host restatement reproduces it bit for bit.  For normal x > 0 the
+// result is within 2 ulp of 1/sqrt(x).  The spiky gradient takes it in place
+// of a square root and a divide: one pass of FP32 arithmetic that also runs
+// on FP32x2 pairs.
+constexpr uint32_t kRsqrtSeed = 0x5f375a86u;
+__device__ __forceinline__ float rsqrt_seed(float x) {
+    return __uint_as_float(kRsqrtSeed - (__float_as_uint(x) >> 1));
+}
+__device__ __forceinline__ float rsqrt_nt(float x) {
+    const float nxh = fmul(-0.5f, x);
+    float y = rsqrt_seed(x);
+#pragma unroll
+    for (int it = 0; it < 3; ++it) y = fmul(y, ffma(fmul(nxh, y), y, 1.5f));
+    return y;
+}
+__device__ __forceinline__ f32x2 rsqrt_nt2(f32x2 x) {
+    float a, b;
+    unpack2(x, a, b);
+    const f32x2 nxh = mul2(splat2(-0.5f), x);
+    f32x2 y = pack2(rsqrt_seed(a), rsqrt_seed(b));
+#pragma unroll
+    for (int it = 0; it < 3; ++it) y = mul2(y, fma2(mul2(nxh, y), y, splat2(1.5f)));
+    return y;
+}
+
+// Below this squared separation (2^-100, separations under 2^-50) the
+// gradient is zero, as for coincident particles; the Newton seed needs a
+// normal input.
+constexpr float kSpikyMinD2 = 7.8886090522101181e-31f;
+
+// spikyGradientFromDistanceSquared (include/pbf/sph_helpers.cuh:48-81):
+// c_spiky (1 - r/h)^2 d / r, zero outside 0 < r < h, with r = d2 / sqrt(d2)
+// and 1/r from rsqrt_nt: g = d * s, s = c_spiky t^2 * rsqrt(d2).
+__device__ __forceinline__ float spiky_scale(const KernelConst& k, float d2) {
+    const float rr = rsqrt_nt(d2);
+    const float r = fmul(d2, rr);
+    const float t = ffma(-r, k.inv_h, 1.0f);
+    return fmul(fmul(k.c_spiky, fmul(t, t)), rr);
+}
 __device__ __forceinline__ void spiky(const KernelConst& k, float dx, float dy, float dz,
                                       float d2, float& gx, float& gy, float& gz) {
-    const float r = fsqrt(d2);
-    if (r <= 0.0f || r >= k.h) {
+    if (d2 < kSpikyMinD2 || d2 >= k.h2) {
         gx = gy = gz = 0.0f;
         return;
     }
-    const float inv_r = fdiv(1.0f, r);
-    const float t = ffma(-r, k.inv_h, 1.0f);
-    const float mag = fmul(k.c_spiky, fmul(t, t));
-    gx = fmul(fmul(dx, inv_r), mag);
-    gy = fmul(fmul(dy, inv_r), mag);
-    gz = fmul(fmul(dz, inv_r), mag);
+    const float s = spiky_scale(k, d2);
+    gx = fmul(dx, s);
+    gy = fmul(dy, s);
+    gz = fmul(dz, s);
+}
+// The scale s of two squared distances, 0 where spiky() returns zero
+// (d * 0 may then be -0, which leaves every sum it enters unchanged).
+__device__ __forceinline__ f32x2 spiky_scale2(const KernelConst& k, f32x2 d2) {
+    const f32x2 rr = rsqrt_nt2(d2);
+    const f32x2 r = mul2(d2, rr);
+    const f32x2 t = fma2(r, splat2(-k.inv_h), splat2(1.0f));
+    const f32x2 sc = mul2(mul2(splat2(k.c_spiky), mul2(t, t)), rr);
+    float a, b, da, db;
+    unpack2(sc, a, b);
+    unpack2(d2, da, db);
+    if (da < kSpikyMinD2 || da >= k.h2) a = 0.0f;
+    if (db < kSpikyMinD2 || db >= k.h2) b = 0.0f;
+    return pack2(a, b);
 }
 
 // Artificial pressure s_corr = -k (W(r)/W(dq))^n with the poly6 normalisation
@@ -164,6 +235,27 @@ __device__ __forceinline__ float ipow_c(float b) {
     return ipow(b, N);
 }
 
+template <int N>
+__device__ __forceinline__ f32x2 ipow_c2(f32x2 b) {
+    if (N == 1) return b;
+    if (N == 2) return mul2(b, b);
+    if (N == 3) return mul2(b, mul2(b, b));
+    if (N == 4) {
+        const f32x2 b2 = mul2(b, b);
+        return mul2(b2, b2);
+    }
+    return b;  // not reached: other exponents use the run-time loop
+}
+__device__ __forceinline__ f32x2 ipow2(f32x2 b, int n) {
+    f32x2 r = splat2(1.0f);
+    while (n > 0) {
+        if (n & 1) r = mul2(r, b);
+        n >>= 1;
+        if (n) b = mul2(b, b);
+    }
+    return r;
+}
+
 // N > 0: exponent fixed at compile time; N == 0: exponent read from s.n.
 template <int N = 0>
 __device__ __forceinline__ float scorr(const ScorrConst& s, float d2) {
@@ -172,6 +264,21 @@ __device__ __forceinline__ float scorr(const ScorrConst& s, float d2) {
     const float ratio = fmul(fsub(s.h2, d2), s.inv_den);
     const float r3 = fmul(fmul(ratio, ratio), ratio);
     return fmul(s.negk, N > 0 ? ipow_c<N>(r3) : ipow(r3, s.n));
+}
+
+// scorr of two squared distances (lane-wise identical to scorr<N>).
+template <int N = 0>
+__device__ __forceinline__ f32x2 scorr2(const ScorrConst& s, f32x2 d2) {
+    if (s.k == 0.0f || s.n <= 0 || s.dq2 >= s.h2) return splat2(0.0f);
+    const f32x2 ratio = mul2(sub2(splat2(s.h2), d2), splat2(s.inv_den));
+    const f32x2 r3 = mul2(mul2(ratio, ratio), ratio);
+    const f32x2 p = (N >= 1 && N <= 4) ? ipow_c2<N>(r3) : ipow2(r3, s.n);
+    float a, b, da, db;
+    unpack2(mul2(splat2(s.negk), p), a, b);
+    unpack2(d2, da, db);
+    if (da >= s.h2) a = 0.0f;
+    if (db >= s.h2) b = 0.0f;
+    return pack2(a, b);
 }
 
 // Grid geometry: cell = floor((p - min) / cellSize) per axis with an IEEE

@@ -353,8 +353,8 @@ struct pbf_solver {
             if (vort) {
                 const int om = take();
                 M(kStVorticity);
-                launch_vorticity(P(rx), P(rv), nbr.as<uint32_t>(), cnt.as<int>(), c, N, P(om), sp,
-                                 st);
+                launch_vorticity(P(rx), P(rv), nbr.as<uint32_t>(), cnt.as<int>(), c, N, P(om), true,
+                                 sp, st);
                 const int t = take();
                 M(kStConfine);
                 launch_confine(P(rx), nbr.as<uint32_t>(), cnt.as<int>(), P(om), P(rv), c, N, P(t),

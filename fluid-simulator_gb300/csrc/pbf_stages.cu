@@ -323,7 +323,7 @@ pbf_status pbf_vorticity(const pbf_float4* positions, const pbf_float4* velociti
         DeviceBuffer dout(count * sizeof(float4));
         const StepConst c = kernel_const(h, 1.0f, 1.0f, max_neighbors, stride);
         launch_vorticity(dpos.as<float4>(), dv.as<float4>(), dnb.as<uint32_t>(), dcnt.as<int>(), c,
-                         static_cast<int>(count), dout.as<float4>(), nullptr, nullptr);
+                         static_cast<int>(count), dout.as<float4>(), false, nullptr, nullptr);
         cuda_check(cudaGetLastError());
         cuda_check(cudaDeviceSynchronize());
         download(reinterpret_cast<float4*>(omega), dout, count);
@@ -347,6 +347,7 @@ pbf_status pbf_confinement(const pbf_float4* positions, const uint32_t* neighbor
         StepConst c = kernel_const(h, 1.0f, 1.0f, max_neighbors, stride);
         c.dt = dt;
         c.vort_eps = strength;
+        launch_omega_norm(dom.as<float4>(), static_cast<int>(count), nullptr);
         launch_confine(dpos.as<float4>(), dnb.as<uint32_t>(), dcnt.as<int>(), dom.as<float4>(),
                        dv.as<float4>(), c, static_cast<int>(count), dout.as<float4>(), nullptr,
                        false, nullptr, nullptr);

@@ -77,16 +77,32 @@ struct F32 {
         const T t3 = t2 * t;
         return c_poly6 * t3;
     }
-    // spikyGradientFromDistanceSquared (include/pbf/sph_helpers.cuh:48-81).
+    // Reciprocal square root by Newton's method from the bit-level seed of
+    // C. Lomont, "Fast Inverse Square Root" (2003), constant 0x5f375a86:
+    // three steps y <- y (3/2 - (x/2) y^2) as multiply / fma, the sequence of
+    // the CUDA kernels.
+    static T rsqrt_nt(T x) {
+        uint32_t bits;
+        std::memcpy(&bits, &x, sizeof bits);
+        bits = 0x5f375a86u - (bits >> 1);
+        T y;
+        std::memcpy(&y, &bits, sizeof y);
+        const T nxh = -0.5f * x;
+        for (int it = 0; it < 3; ++it) y = y * std::fma(nxh * y, y, 1.5f);
+        return y;
+    }
+    // spikyGradientFromDistanceSquared (include/pbf/sph_helpers.cuh:48-81):
+    // g = d * s, s = c_spiky (1 - r/h)^2 / r with r = d2 * rsqrt(d2); zero
+    // for d2 >= h^2 and for d2 < 2^-100 (coincident within 2^-50).
     void spiky(T dx, T dy, T dz, T d2, T g[3]) const {
-        const T r = std::sqrt(d2);
-        if (r <= 0.0f || r >= h) { g[0] = g[1] = g[2] = 0.0f; return; }
-        const T inv_r = 1.0f / r;
+        if (d2 < 7.8886090522101181e-31f || d2 >= h2) { g[0] = g[1] = g[2] = 0.0f; return; }
+        const T rr = rsqrt_nt(d2);
+        const T r = d2 * rr;
         const T t = std::fma(-r, inv_h, 1.0f);
-        const T mag = c_spiky * (t * t);
-        g[0] = (dx * inv_r) * mag;
-        g[1] = (dy * inv_r) * mag;
-        g[2] = (dz * inv_r) * mag;
+        const T s = (c_spiky * (t * t)) * rr;
+        g[0] = dx * s;
+        g[1] = dy * s;
+        g[2] = dz * s;
     }
     static T fma_(T a, T b, T c) { return std::fma(a, b, c); }
     // a.y*b.z - a.z*b.y with one rounding of the product a.y*b.z.
