@@ -126,6 +126,30 @@ class SimulationParams:
         return d
 
 
+class _Scene(C.Structure):
+    _fields_ = [("count", C.c_size_t), ("minBounds", Float3), ("maxBounds", Float3),
+                ("restDensity", C.c_float), ("particleMass", C.c_float),
+                ("xsphViscosity", C.c_float)]
+
+
+@dataclasses.dataclass
+class Scene:
+    """One scene of a batched solver (pbf_scene): its particle count,
+    container bounds and the parameters that may differ between scenes."""
+
+    count: int
+    minBounds: Sequence[float]
+    maxBounds: Sequence[float]
+    restDensity: float
+    particleMass: float
+    xsphViscosity: float
+
+    def to_struct(self) -> _Scene:
+        return _Scene(int(self.count), Float3(*map(float, self.minBounds)),
+                      Float3(*map(float, self.maxBounds)), float(self.restDensity),
+                      float(self.particleMass), float(self.xsphViscosity))
+
+
 _lib = None
 _vp = C.c_void_p
 
@@ -162,6 +186,9 @@ def _declare(L):
         "pbf_copy_positions_device": ([_vp, _vp, sz], S),
         "pbf_copy_velocities_device": ([_vp, _vp, sz], S),
         "pbf_particle_count": ([_vp], sz),
+        "pbf_batch_initialize": ([_vp, C.POINTER(_Scene), C.c_int, C.POINTER(_Params), C.c_int],
+                                 S),
+        "pbf_batch_scene_count": ([_vp], C.c_int),
         "pbf_set_stream": ([_vp, _vp], S),
         "pbf_density_error": ([_vp, C.POINTER(C.c_double), C.POINTER(C.c_double)], S),
         "pbf_copy_working_state": ([_vp, _vp, _vp, _vp, sz], S),
@@ -314,6 +341,19 @@ class PBFSolver:
                                            _f3(max_bounds), C.byref(self._params),
                                            int(max_neighbors))
         self._check(st)
+
+    def initialize_batch(self, scenes: Sequence[Scene], common: SimulationParams,
+                         max_neighbors: int = 256):
+        """pbf_batch_initialize: the scenes step together; particles are set
+        and copied as the concatenation of all scenes in order."""
+        self._params = common.to_struct()
+        arr = (_Scene * len(scenes))(*[sc.to_struct() for sc in scenes])
+        self._scenes = arr
+        self._check(self._L.pbf_batch_initialize(self._h, arr, len(scenes),
+                                                 C.byref(self._params), int(max_neighbors)))
+
+    def scene_count(self) -> int:
+        return int(self._L.pbf_batch_scene_count(self._h))
 
     def set_particles(self, positions, velocities, count: Optional[int] = None):
         if positions is None or velocities is None:

@@ -37,9 +37,44 @@ __device__ __forceinline__ bool fatal(const unsigned* status) {
     return status != nullptr && (__ldcg(status) & kStatusFatalMask) != 0u;
 }
 
+// The scene of particle slot i in a batched solver.
+__device__ __forceinline__ const SceneConst& scene_of(const StepConst& c, int i) {
+    return c.scenes[__ldg(&c.sid[i])];
+}
+
+// Grid and first global cell key of slot i: the scene's (B) or c.g.
+template <bool B>
+__device__ __forceinline__ void grid_of(const StepConst& c, int i, GridConst& g, uint32_t& base) {
+    if constexpr (B) {
+        const SceneConst& s = scene_of(c, i);
+        g = s.g;
+        base = s.cell_base;
+    } else {
+        g = c.g;
+        base = 0u;
+    }
+}
+
+// Colliders with the container of slot i's scene (B) or c.col.
+template <bool B>
+__device__ __forceinline__ Colliders colliders_of(const StepConst& c, int i) {
+    Colliders col = c.col;
+    if constexpr (B) {
+        const SceneConst& s = scene_of(c, i);
+        col.cminx = s.cminx;
+        col.cminy = s.cminy;
+        col.cminz = s.cminz;
+        col.cmaxx = s.cmaxx;
+        col.cmaxy = s.cmaxy;
+        col.cmaxz = s.cmaxz;
+    }
+    return col;
+}
+
 // ---------------------------------------------------------------------------
 // integrate + collision input velocity + keys of the first rebuild
 // ---------------------------------------------------------------------------
+template <bool B>
 __global__ void __launch_bounds__(kBlock)
 k_predict(const float4* __restrict__ x, const float4* __restrict__ v, float4* __restrict__ xs,
           float4* __restrict__ vin, uint32_t* __restrict__ keys, int n, StepConst c,
@@ -58,7 +93,10 @@ k_predict(const float4* __restrict__ x, const float4* __restrict__ v, float4* __
     q.w = p.w;
     xs[i] = q;
     vin[i] = vv;
-    keys[i] = key_of(c.g, q);
+    GridConst g;
+    uint32_t base;
+    grid_of<B>(c, i, g, base);
+    keys[i] = base + key_of(g, q);
 }
 
 __global__ void __launch_bounds__(kBlock)
@@ -195,15 +233,19 @@ __device__ __forceinline__ void lambda_add2(const KernelConst& k, LambdaAcc& a, 
     a.gz = fadd(fadd(a.gz, z0), z1);
 }
 
-__device__ __forceinline__ float lambda_finish(const StepConst& c, const LambdaAcc& a) {
-    const float rho = fmul(c.mass, a.wsum);
+__device__ __forceinline__ float lambda_finish(float mass, float rho0, float gs2, float eps,
+                                               const LambdaAcc& a) {
+    const float rho = fmul(mass, a.wsum);
     const float g2 = dist2(a.gx, a.gy, a.gz);
-    const float denom = ffma(c.gs2, fadd(a.s2, g2), c.lambda_eps);
-    const float C = fsub(fdiv(rho, c.rho0), 1.0f);
+    const float denom = ffma(gs2, fadd(a.s2, g2), eps);
+    const float C = fsub(fdiv(rho, rho0), 1.0f);
     return fdiv(-C, denom);
 }
+__device__ __forceinline__ float lambda_finish(const StepConst& c, const LambdaAcc& a) {
+    return lambda_finish(c.mass, c.rho0, c.gs2, c.lambda_eps, a);
+}
 
-template <bool LAMBDA>
+template <bool LAMBDA, bool B>
 __global__ void __launch_bounds__(kBlock)
 k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
          const float* __restrict__ sy, const float* __restrict__ sz, const int* __restrict__ first,
@@ -212,16 +254,19 @@ k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || fatal(status)) return;
     const float4 pi = xs[i];
+    GridConst g;
+    uint32_t base;
+    grid_of<B>(c, i, g, base);
     int cx, cy, cz;
-    cell_of(c.g, pi.x, pi.y, pi.z, cx, cy, cz);
-    const int R = c.g.radius;
-    const int x0 = max(0, cx - R), x1 = min(c.g.gx - 1, cx + R);
-    const int y0 = max(0, cy - R), y1 = min(c.g.gy - 1, cy + R);
-    const int z0 = max(0, cz - R), z1 = min(c.g.gz - 1, cz + R);
+    cell_of(g, pi.x, pi.y, pi.z, cx, cy, cz);
+    const int R = g.radius;
+    const int x0 = max(0, cx - R), x1 = min(g.gx - 1, cx + R);
+    const int y0 = max(0, cy - R), y1 = min(g.gy - 1, cy + R);
+    const int z0 = max(0, cz - R), z1 = min(g.gz - 1, cz + R);
     // Keys fit in 32 bits (cells < 2^32 is checked at initialisation), so
     // the reference's 64-bit key arithmetic truncates to the same values.
-    const uint32_t gx = static_cast<uint32_t>(c.g.gx);
-    const uint32_t gxy = gx * static_cast<uint32_t>(c.g.gy);
+    const uint32_t gx = static_cast<uint32_t>(g.gx);
+    const uint32_t gxy = gx * static_cast<uint32_t>(g.gy);
     const float h2 = c.k.h2;
     const int max_nb = c.max_nb;
     uint32_t* __restrict__ out = nbr + i;
@@ -239,7 +284,8 @@ k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
     // are padded so the odd element past e is always readable.
     for (int z = z0; z <= z1; ++z) {
         for (int y = y0; y <= y1; ++y) {
-            const uint32_t row = static_cast<uint32_t>(y) * gx + static_cast<uint32_t>(z) * gxy;
+            const uint32_t row =
+                base + static_cast<uint32_t>(y) * gx + static_cast<uint32_t>(z) * gxy;
             const int s = __ldg(&first[row + static_cast<uint32_t>(x0)]);
             const int e = __ldg(&first[row + static_cast<uint32_t>(x1) + 1u]);
             for (int j0 = s & ~1; j0 < e; j0 += 32) {
@@ -302,7 +348,12 @@ k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
             const float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y), dz = fsub(pi.z, pj.z);
             lambda_add(c.k, acc, dx, dy, dz, dist2(dx, dy, dz));
         }
-        lam[i] = lambda_finish(c, acc);
+        if constexpr (B) {
+            const SceneConst& sc = scene_of(c, i);
+            lam[i] = lambda_finish(sc.mass, sc.rho0, sc.gs2, c.lambda_eps, acc);
+        } else {
+            lam[i] = lambda_finish(c, acc);
+        }
     }
 }
 
@@ -400,7 +451,8 @@ template <int N>
 __device__ __forceinline__ void delta_sum(const StepConst& c, const float4* __restrict__ xs,
                                           const uint32_t* __restrict__ nbr,
                                           const float* __restrict__ lam, int i, int count,
-                                          float4 pi, float& dpx, float& dpy, float& dpz) {
+                                          float4 pi, float gs, float& dpx, float& dpy,
+                                          float& dpz) {
     const float li = lam[i];
     float ax = 0.0f, ay = 0.0f, az = 0.0f;
     for_each_neighbor_pair<PosLam>(
@@ -410,14 +462,14 @@ __device__ __forceinline__ void delta_sum(const StepConst& c, const float4* __re
             delta_term2<N>(c, pi, li, a.p, a.l, b.p, b.l, ax, ay, az);
         },
         [&](const PosLam& q) { delta_term<N>(c, pi, li, q.p, q.l, ax, ay, az); });
-    dpx = fmul(c.gs, ax);
-    dpy = fmul(c.gs, ay);
-    dpz = fmul(c.gs, az);
+    dpx = fmul(gs, ax);
+    dpy = fmul(gs, ay);
+    dpz = fmul(gs, az);
 }
 
 // delta p + applyDeltaPosition + CollisionSystem::solve + next cell keys.
 // N: artificial-pressure exponent fixed at compile time (0 = read at run time).
-template <int N>
+template <int N, bool B>
 __global__ void __launch_bounds__(kBlock)
 k_delta_apply(const float4* __restrict__ xs, const uint32_t* __restrict__ nbr,
               const int* __restrict__ cnt, const float* __restrict__ lam, StepConst c, int n,
@@ -431,14 +483,20 @@ k_delta_apply(const float4* __restrict__ xs, const uint32_t* __restrict__ nbr,
     if (!count_ok(count, c.max_nb)) {
         dpx = dpy = dpz = CUDART_NAN_F;
     } else {
-        delta_sum<N>(c, xs, nbr, lam, i, count, pi, dpx, dpy, dpz);
+        const float gs = B ? scene_of(c, i).gs : c.gs;
+        delta_sum<N>(c, xs, nbr, lam, i, count, pi, gs, dpx, dpy, dpz);
     }
     float px = fadd(pi.x, dpx), py = fadd(pi.y, dpy), pz = fadd(pi.z, dpz);
-    if (!project_all(c.col, c.particle_radius, px, py, pz))
+    if (!project_all(colliders_of<B>(c, i), c.particle_radius, px, py, pz))
         atomicOr(status, kStatusNotConverged);
     const float4 q = make_float4(px, py, pz, pi.w);
     xs_out[i] = q;
-    if (keys_out) keys_out[i] = key_of(c.g, q);
+    if (keys_out) {
+        GridConst g;
+        uint32_t base;
+        grid_of<B>(c, i, g, base);
+        keys_out[i] = base + key_of(g, q);
+    }
 }
 
 // Gather x, v_in, v.w and ids through the composite permutation of the
@@ -468,7 +526,8 @@ k_finalize(const uint32_t* __restrict__ org, const float4* __restrict__ x_old,
 // applyXsphViscosity (pbf_solver_kernels.cu:213-266).
 __device__ __forceinline__ float4 xsph_one(const StepConst& c, const float4* __restrict__ x,
                                            const float4* __restrict__ v,
-                                           const uint32_t* __restrict__ nbr, int count, int i) {
+                                           const uint32_t* __restrict__ nbr, int count, int i,
+                                           float xsph_c) {
     const float4 vi = v[i];
     if (!count_ok(count, c.max_nb))
         return make_float4(CUDART_NAN_F, CUDART_NAN_F, CUDART_NAN_F, vi.w);
@@ -496,10 +555,11 @@ __device__ __forceinline__ float4 xsph_one(const StepConst& c, const float4* __r
             cy = ffma(fsub(q.v.y, vi.y), w, cy);
             cz = ffma(fsub(q.v.z, vi.z), w, cz);
         });
-    return make_float4(ffma(c.xsph_c, cx, vi.x), ffma(c.xsph_c, cy, vi.y),
-                       ffma(c.xsph_c, cz, vi.z), vi.w);
+    return make_float4(ffma(xsph_c, cx, vi.x), ffma(xsph_c, cy, vi.y), ffma(xsph_c, cz, vi.z),
+                       vi.w);
 }
 
+template <bool B>
 __global__ void __launch_bounds__(kBlock)
 k_xsph(const float4* __restrict__ x, const float4* __restrict__ v,
        const uint32_t* __restrict__ nbr, const int* __restrict__ cnt, StepConst c, int n,
@@ -507,9 +567,10 @@ k_xsph(const float4* __restrict__ x, const float4* __restrict__ v,
        const unsigned* __restrict__ status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || fatal(status)) return;
-    float4 out = xsph_one(c, x, v, nbr, cnt[i], i);
+    float4 out = xsph_one(c, x, v, nbr, cnt[i], i, B ? scene_of(c, i).xsph_c : c.xsph_c);
     if (resolve)
-        resolve_velocity(c.col, c.particle_radius, c.restitution, c.friction, x[i], vin[i], out);
+        resolve_velocity(colliders_of<B>(c, i), c.particle_radius, c.restitution, c.friction,
+                         x[i], vin[i], out);
     v_out[i] = out;
 }
 
@@ -619,6 +680,7 @@ __device__ __forceinline__ float4 confine_one(const StepConst& c, const float4* 
     return make_float4(ffma(c.dt, cx, vi.x), ffma(c.dt, cy, vi.y), ffma(c.dt, cz, vi.z), vi.w);
 }
 
+template <bool B>
 __global__ void __launch_bounds__(kBlock)
 k_confine(const float4* __restrict__ x, const uint32_t* __restrict__ nbr,
           const int* __restrict__ cnt, const float4* __restrict__ om,
@@ -628,17 +690,20 @@ k_confine(const float4* __restrict__ x, const uint32_t* __restrict__ nbr,
     if (i >= n || fatal(status)) return;
     float4 out = confine_one(c, x, nbr, cnt[i], om, v, i);
     if (resolve)
-        resolve_velocity(c.col, c.particle_radius, c.restitution, c.friction, x[i], vin[i], out);
+        resolve_velocity(colliders_of<B>(c, i), c.particle_radius, c.restitution, c.friction,
+                         x[i], vin[i], out);
     v_out[i] = out;
 }
 
+template <bool B>
 __global__ void __launch_bounds__(kBlock)
 k_resolve(const float4* __restrict__ x, const float4* __restrict__ vin, float4* __restrict__ v,
           StepConst c, int n, const unsigned* __restrict__ status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || fatal(status)) return;
     float4 vv = v[i];
-    resolve_velocity(c.col, c.particle_radius, c.restitution, c.friction, x[i], vin[i], vv);
+    resolve_velocity(colliders_of<B>(c, i), c.particle_radius, c.restitution, c.friction, x[i],
+                     vin[i], vv);
     v[i] = vv;
 }
 
@@ -668,7 +733,9 @@ k_density(const float4* __restrict__ x, const uint32_t* __restrict__ nbr,
         const float4 pj = __ldg(&x[__ldg(&nbr[static_cast<size_t>(k) * c.stride + i])]);
         wsum = fadd(wsum, poly6(c.k, dist2(fsub(pi.x, pj.x), fsub(pi.y, pj.y), fsub(pi.z, pj.z))));
     }
-    err[i] = fabsf(fsub(fdiv(fmul(c.mass, wsum), c.rho0), 1.0f));
+    const float mass = c.scenes ? scene_of(c, i).mass : c.mass;
+    const float rho0 = c.scenes ? scene_of(c, i).rho0 : c.rho0;
+    err[i] = fabsf(fsub(fdiv(fmul(mass, wsum), rho0), 1.0f));
 }
 
 // --- stage kernels -----------------------------------------------------------
@@ -710,7 +777,7 @@ k_delta_list(const float4* __restrict__ xs, const uint32_t* __restrict__ nbr,
         return;
     }
     float dx, dy, dz;
-    delta_sum<0>(c, xs, nbr, lam, i, count, xs[i], dx, dy, dz);
+    delta_sum<0>(c, xs, nbr, lam, i, count, xs[i], c.gs, dx, dy, dz);
     delta[i] = make_float4(dx, dy, dz, 0.0f);
 }
 
@@ -751,7 +818,10 @@ k_integrate(const float4* __restrict__ x, float4* __restrict__ xs, float4* __res
 // --- launchers ---------------------------------------------------------------
 void launch_predict(const float4* x, const float4* v, float4* xs, float4* vin, uint32_t* keys,
                     int n, const StepConst& c, const unsigned* status, cudaStream_t st) {
-    launch_k(k_predict, blocks_for(n), kBlock, st, x, v, xs, vin, keys, n, c, status);
+    if (c.scenes)
+        launch_k(k_predict<true>, blocks_for(n), kBlock, st, x, v, xs, vin, keys, n, c, status);
+    else
+        launch_k(k_predict<false>, blocks_for(n), kBlock, st, x, v, xs, vin, keys, n, c, status);
 }
 void launch_cell_ranges(const uint32_t* skeys, int* cs, int* ce, int n, const unsigned* status,
                         cudaStream_t st) {
@@ -774,36 +844,61 @@ void launch_gather_first(const uint32_t* perm, const float4* xs_in, float4* xs_o
 void launch_search(const float4* xs, const float* sx, const float* sy, const float* sz,
                    const int* first, const StepConst& c, int n, uint32_t* nbr, int* cnt, float* lam,
                    unsigned* status, bool with_lambda, cudaStream_t st) {
-    if (with_lambda)
-        launch_k(k_search<true>, blocks_for(n), kBlock, st, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
-                                                         status);
+    const unsigned g = blocks_for(n);
+    if (with_lambda && c.scenes)
+        launch_k(k_search<true, true>, g, kBlock, st, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
+                 status);
+    else if (with_lambda)
+        launch_k(k_search<true, false>, g, kBlock, st, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
+                 status);
+    else if (c.scenes)
+        launch_k(k_search<false, true>, g, kBlock, st, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
+                 status);
     else
-        launch_k(k_search<false>, blocks_for(n), kBlock, st, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
-                                                          status);
+        launch_k(k_search<false, false>, g, kBlock, st, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
+                 status);
+}
+
+template <bool B>
+void launch_delta_apply_b(const float4* xs, const uint32_t* nbr, const int* cnt, const float* lam,
+                          const StepConst& c, int n, float4* xs_out, uint32_t* keys_out,
+                          unsigned* status, cudaStream_t st) {
+    const unsigned g = blocks_for(n);
+#define PBF_DELTA_CASE(N)                                                                        \
+    launch_k(k_delta_apply<N, B>, g, kBlock, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out, status)
+    switch (c.sc.k != 0.0f ? c.sc.n : 0) {
+        case 1: PBF_DELTA_CASE(1); break;
+        case 2: PBF_DELTA_CASE(2); break;
+        case 3: PBF_DELTA_CASE(3); break;
+        case 4: PBF_DELTA_CASE(4); break;
+        default: PBF_DELTA_CASE(0); break;
+    }
+#undef PBF_DELTA_CASE
 }
 void launch_delta_apply(const float4* xs, const uint32_t* nbr, const int* cnt, const float* lam,
                         const StepConst& c, int n, float4* xs_out, uint32_t* keys_out,
                         unsigned* status, cudaStream_t st) {
-    const unsigned g = blocks_for(n);
-    switch (c.sc.k != 0.0f ? c.sc.n : 0) {
-        case 1: launch_k(k_delta_apply<1>, g, kBlock, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out, status); break;
-        case 2: launch_k(k_delta_apply<2>, g, kBlock, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out, status); break;
-        case 3: launch_k(k_delta_apply<3>, g, kBlock, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out, status); break;
-        case 4: launch_k(k_delta_apply<4>, g, kBlock, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out, status); break;
-        default: launch_k(k_delta_apply<0>, g, kBlock, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out, status); break;
-    }
+    if (c.scenes)
+        launch_delta_apply_b<true>(xs, nbr, cnt, lam, c, n, xs_out, keys_out, status, st);
+    else
+        launch_delta_apply_b<false>(xs, nbr, cnt, lam, c, n, xs_out, keys_out, status, st);
 }
 void launch_finalize(const uint32_t* org, const float4* x_old, const float4* vin_old,
                      const float4* v_old, const uint32_t* id_old, const float4* xs, int n,
                      const StepConst& c, float4* v_new, float4* vin_new, uint32_t* id_new,
                      const unsigned* status, cudaStream_t st) {
     launch_k(k_finalize, blocks_for(n), kBlock, st, org, x_old, vin_old, v_old, id_old, xs, n, c,
-                                                 v_new, vin_new, id_new, status);
+             v_new, vin_new, id_new, status);
 }
 void launch_xsph(const float4* x, const float4* v, const uint32_t* nbr, const int* cnt,
                  const StepConst& c, int n, float4* v_out, const float4* vin, bool resolve,
                  const unsigned* status, cudaStream_t st) {
-    launch_k(k_xsph, blocks_for(n), kBlock, st, x, v, nbr, cnt, c, n, v_out, vin, resolve, status);
+    if (c.scenes)
+        launch_k(k_xsph<true>, blocks_for(n), kBlock, st, x, v, nbr, cnt, c, n, v_out, vin, resolve,
+                 status);
+    else
+        launch_k(k_xsph<false>, blocks_for(n), kBlock, st, x, v, nbr, cnt, c, n, v_out, vin,
+                 resolve, status);
 }
 void launch_vorticity(const float4* x, const float4* v, const uint32_t* nbr, const int* cnt,
                       const StepConst& c, int n, float4* omega, bool store_norm,
@@ -817,12 +912,19 @@ void launch_omega_norm(float4* omega, int n, cudaStream_t st) {
 void launch_confine(const float4* x, const uint32_t* nbr, const int* cnt, const float4* omega,
                     const float4* v, const StepConst& c, int n, float4* v_out,
                     const float4* vin, bool resolve, const unsigned* status, cudaStream_t st) {
-    launch_k(k_confine, blocks_for(n), kBlock, st, x, nbr, cnt, omega, v, c, n, v_out, vin,
-             resolve, status);
+    if (c.scenes)
+        launch_k(k_confine<true>, blocks_for(n), kBlock, st, x, nbr, cnt, omega, v, c, n, v_out,
+                 vin, resolve, status);
+    else
+        launch_k(k_confine<false>, blocks_for(n), kBlock, st, x, nbr, cnt, omega, v, c, n, v_out,
+                 vin, resolve, status);
 }
 void launch_resolve(const float4* x, const float4* vin, float4* v, const StepConst& c, int n,
                     const unsigned* status, cudaStream_t st) {
-    launch_k(k_resolve, blocks_for(n), kBlock, st, x, vin, v, c, n, status);
+    if (c.scenes)
+        launch_k(k_resolve<true>, blocks_for(n), kBlock, st, x, vin, v, c, n, status);
+    else
+        launch_k(k_resolve<false>, blocks_for(n), kBlock, st, x, vin, v, c, n, status);
 }
 void launch_scatter_by_id(const float4* vals, const uint32_t* id, float4* out, int n,
                           cudaStream_t st) {

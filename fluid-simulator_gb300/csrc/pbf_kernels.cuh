@@ -10,6 +10,16 @@
 
 namespace pbf {
 
+// Per-scene constants of a batched solver: the scene's own grid (its cell
+// keys are offset by cell_base, so one sort orders all scenes, scene by
+// scene), its container and the density terms that vary between scenes.
+struct SceneConst {
+    GridConst g;
+    uint32_t cell_base;
+    float cminx, cminy, cminz, cmaxx, cmaxy, cmaxz;
+    float rho0, mass, gs, gs2, xsph_c;
+};
+
 // Everything a step kernel needs, passed by value.
 struct StepConst {
     KernelConst k;
@@ -23,6 +33,10 @@ struct StepConst {
     float xsph_c, vort_eps;
     int max_nb;
     size_t stride;  // slot stride of the neighbour lists
+    // Batched solver: scene table and the scene of every particle slot
+    // (scenes occupy fixed contiguous slot ranges); null for one scene.
+    const SceneConst* scenes;
+    const uint16_t* sid;
 };
 
 constexpr int kBlock = 256;

@@ -149,6 +149,13 @@ struct pbf_solver {
     DeviceBuffer d_colliders;
     bool colliders_dirty = true;
 
+    // Batched mode (nscenes > 0): scenes occupy fixed slot ranges
+    // [scene_off[s], scene_off[s + 1]); every kernel reads its scene's grid,
+    // container and density terms from scene_tab through scene_id.
+    int nscenes = 0;
+    std::vector<size_t> scene_off;
+    DeviceBuffer scene_tab, scene_id;
+
     // Device state.
     DeviceBuffer f4[kF4Pool];
     DeviceBuffer ids[2], org[2];
@@ -237,6 +244,10 @@ struct pbf_solver {
         c.col.cmaxx = mx.x;
         c.col.cmaxy = mx.y;
         c.col.cmaxz = mx.z;
+        if (nscenes > 0) {
+            c.scenes = scene_tab.as<SceneConst>();
+            c.sid = scene_id.as<uint16_t>();
+        }
         return c;
     }
 
@@ -492,8 +503,18 @@ struct pbf_solver {
         const uint64_t ncells = uint64_t(d[0]) * uint64_t(d[1]) * uint64_t(d[2]);
 
         use_device();
-        // Allocate everything before touching the active configuration, so a
-        // failure leaves the previous solver state intact.
+        allocate_and_commit(max_particles, strd, maxnb, ncells, DeviceBuffer(), DeviceBuffer(), {});
+        prm = p;
+        mn = lo;
+        mx = hi;
+        dims = d;
+    }
+
+    // Allocates the device state for `max_particles` slots and `ncells` grid
+    // cells, then makes it (and the scene table, empty for one scene) the
+    // active configuration.  Nothing changes if an allocation fails.
+    void allocate_and_commit(size_t max_particles, size_t strd, int maxnb, uint64_t ncells,
+                             DeviceBuffer ntab, DeviceBuffer nsid, std::vector<size_t> off) {
         const size_t f4b = max_particles * sizeof(float4);
         const size_t u4b = max_particles * sizeof(uint32_t);
         DeviceBuffer nf4[kF4Pool], nids[2], norg[2];
@@ -535,20 +556,107 @@ struct pbf_solver {
         n = 0;
         stride = strd;
         max_nb = maxnb;
-        prm = p;
-        mn = lo;
-        mx = hi;
-        dims = d;
         cells = ncells;
         ix = 0;
         iv = 1;
         iid = 0;
         colliders_dirty = true;
+        scene_tab = std::move(ntab);
+        scene_id = std::move(nsid);
+        scene_off = std::move(off);
+        nscenes = scene_off.empty() ? 0 : static_cast<int>(scene_off.size()) - 1;
+    }
+
+    // Batched initialisation: `count` scenes, each with its own particle
+    // count, container (== grid bounds) and rest density, mass and XSPH
+    // strength; every other parameter is shared.
+    void initialize_batch(const pbf_scene* sc, int count, const pbf_params& common, int maxnb) {
+        if (count <= 0 || sc == nullptr)
+            fail(PBF_ERR_INVALID_ARGUMENT, "A batch needs at least one scene");
+        if (count > 65535) fail(PBF_ERR_LENGTH, "A batch holds at most 65535 scenes");
+        if (maxnb <= 0) fail(PBF_ERR_INVALID_ARGUMENT, "maxNeighbors must be greater than zero");
+        validate_params(common);
+        std::vector<size_t> off(1, 0);
+        std::vector<SceneConst> tab(static_cast<size_t>(count));
+        uint64_t total_cells = 0;
+        const bool xsph_on = sc[0].xsphViscosity != 0.0f;
+        for (int k = 0; k < count; ++k) {
+            const pbf_scene& q = sc[k];
+            if (q.count == 0) fail(PBF_ERR_INVALID_ARGUMENT, "Every scene needs particles");
+            pbf_params p = common;
+            p.restDensity = q.restDensity;
+            p.particleMass = q.particleMass;
+            p.xsphViscosity = q.xsphViscosity;
+            validate_params(p);
+            if ((q.xsphViscosity != 0.0f) != xsph_on)
+                fail(PBF_ERR_INVALID_ARGUMENT,
+                     "XSPH must be enabled in every scene of a batch or in none");
+            const double width = double(q.maxBounds.x) - double(q.minBounds.x);
+            const double depth = double(q.maxBounds.z) - double(q.minBounds.z);
+            const double diameter = 2.0 * double(common.particleRadius);
+            if (width < diameter || depth < diameter)
+                fail(PBF_ERR_INVALID_ARGUMENT,
+                     "Particle diameter exceeds closed container dimensions");
+            const std::array<int, 3> d =
+                grid_dims_checked(q.minBounds, q.maxBounds, common.smoothingRadius);
+            SceneConst& t = tab[static_cast<size_t>(k)];
+            t.g.minx = q.minBounds.x;
+            t.g.miny = q.minBounds.y;
+            t.g.minz = q.minBounds.z;
+            t.g.cell = common.smoothingRadius;
+            t.g.gx = d[0];
+            t.g.gy = d[1];
+            t.g.gz = d[2];
+            t.g.radius = 1;
+            t.cell_base = static_cast<uint32_t>(total_cells);
+            t.cminx = q.minBounds.x;
+            t.cminy = q.minBounds.y;
+            t.cminz = q.minBounds.z;
+            t.cmaxx = q.maxBounds.x;
+            t.cmaxy = q.maxBounds.y;
+            t.cmaxz = q.maxBounds.z;
+            t.rho0 = q.restDensity;
+            t.mass = q.particleMass;
+            t.gs = q.particleMass / q.restDensity;
+            t.gs2 = t.gs * t.gs;
+            t.xsph_c = q.xsphViscosity;
+            total_cells += uint64_t(d[0]) * uint64_t(d[1]) * uint64_t(d[2]);
+            if (total_cells >= (uint64_t(1) << 32))
+                fail(PBF_ERR_LENGTH, "Batch grid exceeds 32-bit key capacity");
+            off.push_back(off.back() + q.count);
+            if (off.back() > static_cast<size_t>(std::numeric_limits<int>::max()))
+                fail(PBF_ERR_LENGTH, "Particle count exceeds CUDA kernel index range");
+        }
+        const size_t total = off.back();
+        const size_t strd = (total + kStrideAlignment - 1) / kStrideAlignment * kStrideAlignment;
+        if (strd > std::numeric_limits<size_t>::max() / size_t(maxnb))
+            fail(PBF_ERR_LENGTH, "Neighbor buffer size overflows size_t");
+        std::vector<uint16_t> sid(total);
+        for (int k = 0; k < count; ++k)
+            std::fill(sid.begin() + off[k], sid.begin() + off[k + 1], static_cast<uint16_t>(k));
+
+        use_device();
+        DeviceBuffer ntab(tab.size() * sizeof(SceneConst)), nsid(total * sizeof(uint16_t));
+        cuda_check(cudaMemcpy(ntab.get(), tab.data(), tab.size() * sizeof(SceneConst),
+                              cudaMemcpyHostToDevice));
+        cuda_check(cudaMemcpy(nsid.get(), sid.data(), total * sizeof(uint16_t),
+                              cudaMemcpyHostToDevice));
+        allocate_and_commit(total, strd, maxnb, total_cells, std::move(ntab), std::move(nsid),
+                            std::move(off));
+        prm = common;
+        prm.restDensity = sc[0].restDensity;
+        prm.particleMass = sc[0].particleMass;
+        prm.xsphViscosity = sc[0].xsphViscosity;
+        mn = sc[0].minBounds;
+        mx = sc[0].maxBounds;
+        dims = {tab[0].g.gx, tab[0].g.gy, tab[0].g.gz};
     }
 
     void set_particles(const float4* pos, const float4* vel, size_t count, bool device_ptrs) {
         require_initialized("PBFSolver must be initialized before setting particles");
         if (count > cap) fail(PBF_ERR_OUT_OF_RANGE, "Particle count exceeds solver capacity");
+        if (nscenes > 0 && count != cap)
+            fail(PBF_ERR_OUT_OF_RANGE, "A batch takes exactly the particles of all its scenes");
         use_device();
         if (count == 0) {
             n = 0;
@@ -853,6 +961,16 @@ pbf_status pbf_copy_velocities_device(pbf_solver* s, pbf_float4* out, size_t cou
 }
 
 size_t pbf_particle_count(const pbf_solver* s) { return s ? s->n : 0; }
+
+pbf_status pbf_batch_initialize(pbf_solver* s, const pbf_scene* scenes, int scene_count,
+                                const pbf_params* common, int max_neighbors) {
+    PBF_GUARD(s, {
+        if (!common) fail(PBF_ERR_INVALID_ARGUMENT, "params must not be null");
+        s->initialize_batch(scenes, scene_count, *common, max_neighbors);
+    });
+}
+
+int pbf_batch_scene_count(const pbf_solver* s) { return s ? s->nscenes : 0; }
 
 pbf_status pbf_set_stream(pbf_solver* s, void* stream) {
     PBF_GUARD(s, {

@@ -10,6 +10,12 @@ then y, then z; w = 1.
   box [0,12.8]x[0,6.4]x[0,6.4] (the fluid fills the x<6.4, z<3.2 corner).
 * ``imbalanced_8m``  -- half a dense lattice column, half 16 Gaussian blobs
   (sigma 4h, centres uniform), box 25.6x12.8x12.8.
+* ``batched_scenes`` -- 256 independent dam breaks, particle counts
+  log-uniform in [2,048, 65,536] (seed 7): a (2k, 2k, k) lattice per scene in
+  a (4k, 2k, 2k) x spacing box, rest density x U(0.9, 1.1) with the mass
+  scaled alike, XSPH c ~ U(0.005, 0.05) applied as c * m / rho0 (the
+  reference's XSPH sum carries no m / rho factor, so an unscaled c >= 1e-4
+  overshoots: c * sum W ~ c * rho0 / m).
 * ``reference_benchmark`` -- the scene of the reference's benchmark
   (benchmark/pbf_benchmark.cu:20-114): 262,144 particles in 32 layers of
   128x64 at spacing 0.06 below y = 3.75, container [0,8.2]x[0,4]x[0,4.2], one
@@ -17,6 +23,8 @@ then y, then z; w = 1.
 """
 
 from __future__ import annotations
+
+import dataclasses
 
 import numpy as np
 
@@ -160,3 +168,34 @@ SCENES = {
     "imbalanced_8m": imbalanced_8m,
     "reference_benchmark": reference_benchmark,
 }
+
+
+def batched_scenes(n_scenes: int = 256, n_min: int = 2048, n_max: int = 65536, seed: int = 7):
+    """Returns (scenes, common, positions, velocities, per_scene) where scenes
+    is a list of ``Scene`` records, common the shared SimulationParams,
+    positions / velocities the concatenation in scene order and per_scene a
+    list of (positions, velocities, min_bounds, max_bounds, SimulationParams)
+    for running each scene alone."""
+    from . import Scene
+
+    rng = np.random.default_rng(seed)
+    targets = np.exp(rng.uniform(np.log(n_min), np.log(n_max), n_scenes))
+    common = dam_break_params()
+    scenes, per, P, V = [], [], [], []
+    for s in range(n_scenes):
+        k = max(2, int(round((targets[s] / 4.0) ** (1.0 / 3.0))))
+        nx, ny, nz = 2 * k, 2 * k, k
+        box = (2 * nx * SPACING, ny * SPACING, 2 * nz * SPACING)
+        pos = lattice(nx, ny, nz, SPACING, (RADIUS, RADIUS, RADIUS), 0.01 * H, seed * 1000 + s)
+        vel = np.zeros_like(pos)
+        scale = float(rng.uniform(0.9, 1.1))
+        rho0 = float(np.float32(common.restDensity * scale))
+        mass = float(np.float32(rho0) * np.float32(SPACING) ** 3)
+        c = float(rng.uniform(0.005, 0.05))
+        xsph = float(np.float32(c * mass / rho0))
+        scenes.append(Scene(len(pos), (0.0, 0.0, 0.0), box, rho0, mass, xsph))
+        prm = dataclasses.replace(common, restDensity=rho0, particleMass=mass, xsphViscosity=xsph)
+        per.append((pos, vel, (0.0, 0.0, 0.0), box, prm))
+        P.append(pos)
+        V.append(vel)
+    return scenes, common, np.concatenate(P), np.concatenate(V), per

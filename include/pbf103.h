@@ -118,6 +118,32 @@ pbf_status pbf_copy_velocities_device(pbf_solver* s, pbf_float4* d_velocities, s
 
 size_t pbf_particle_count(const pbf_solver* s);
 
+/* ---- batched scenes (no counterpart in the reference) -------------------
+ * Many independent scenes stepped together: one launch per stage for all of
+ * them.  Each scene has its own particle count, container (== grid bounds,
+ * cell size = smoothingRadius) and rest density, particle mass and XSPH
+ * strength; every other field of `common` is shared.  XSPH must be on in
+ * every scene or in none.  Cell keys are offset per scene, so one stable
+ * sort orders all scenes and each scene's arithmetic is exactly that of a
+ * solver initialised with that scene alone.  The handle then takes
+ * pbf_set_particles with all scenes' particles concatenated in scene order
+ * (the sum of the counts, no fewer), and pbf_step / pbf_run / pbf_copy_*
+ * work on the concatenation.  Colliders set on the handle apply to every
+ * scene in its own coordinates.  pbf_initialize returns the handle to one
+ * scene. */
+typedef struct pbf_scene {
+    size_t count;
+    pbf_float3 minBounds;
+    pbf_float3 maxBounds;
+    float restDensity;
+    float particleMass;
+    float xsphViscosity;
+} pbf_scene;
+pbf_status pbf_batch_initialize(pbf_solver* s, const pbf_scene* scenes, int scene_count,
+                                const pbf_params* common, int max_neighbors);
+/* Scenes of a batched handle (0 after pbf_initialize). */
+int pbf_batch_scene_count(const pbf_solver* s);
+
 /* ---- streams, timing, diagnostics (no counterpart in the reference) ----- */
 /* Run subsequent work on `stream` (a cudaStream_t); NULL restores the solver's
  * own stream.  The solver still synchronises its own calls. */

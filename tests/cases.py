@@ -198,6 +198,24 @@ def case_neighbors_misc(B):
     assert lists == np_brute(far, 1e10)
 
 
+def case_neighbors_nonfinite(B):
+    """Non-finite and huge coordinates: NaN, +-inf (inf - inf is NaN) and
+    +-1e30 never pass d2 <= h2; the finite cluster still finds itself."""
+    inf, nan = np.inf, np.nan
+    pos = np.asarray([[2.0, 2.0, 2.0, 1], [2.1, 2.0, 2.0, 1], [2.0, 2.2, 2.0, 1],
+                      [2.0, 2.0, 2.3, 1], [nan, 2.0, 2.0, 1], [2.0, nan, 2.0, 1],
+                      [inf, 2.0, 2.0, 1], [inf, 2.0, 2.0, 1], [2.0, 2.0, -inf, 1],
+                      [-inf, -inf, -inf, 1], [1e30, 2.0, 2.0, 1], [2.0, 2.0, -1e30, 1],
+                      [4.9, 4.9, inf, 1], [4.9, 4.9, inf, 1]], np.float32)
+    with np.errstate(invalid="ignore", over="ignore"):
+        exp = np_brute(pos, 0.5)
+    counts, lists, ov = run_search(B, pos, 0.5)
+    assert not ov
+    assert lists == exp
+    assert list(counts) == [len(e) for e in exp]
+    assert list(counts[:4]) == [3, 3, 3, 3] and not any(counts[4:])
+
+
 def case_neighbors_cross_boundaries(B):
     """AllSixDirectionsAndDiagonalAcrossCellBoundaries."""
     pos = np.asarray([[2.01, 2.01, 2.01, 1], [1.99, 2.01, 2.01, 1], [2.01, 1.99, 2.01, 1],

@@ -1,0 +1,75 @@
+"""Batched solver on the GPU.
+
+Every scene of a batch must come out bit for bit as the same scene run alone
+by a single-scene solver (itself bit-exact against the FP32 oracle): the
+per-scene key offset keeps each scene's sort order, lists and sums unchanged.
+"""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def run_alone(pbf, per, steps):
+    out = []
+    for p, v, lo, hi, q in per:
+        a = pbf.PBFSolver()
+        a.initialize(len(p), lo, hi, q)
+        a.set_particles(p, v)
+        a.run(steps)
+        out.append((a.copy_positions_to_host(), a.copy_velocities_to_host()))
+        a.close()
+    return out
+
+
+@pytest.mark.parametrize("steps", [1, 6])
+def test_batch_equals_each_scene_alone(pbf, scenes, steps):
+    sc, prm, pos, vel, per = scenes.batched_scenes(n_scenes=12, n_min=512, n_max=8192, seed=11)
+    b = pbf.PBFSolver()
+    b.initialize_batch(sc, prm)
+    assert b.scene_count() == 12
+    b.set_particles(pos, vel)
+    b.run(steps)
+    bp, bv = b.copy_positions_to_host(), b.copy_velocities_to_host()
+    off = 0
+    for k, (ap, av) in enumerate(run_alone(pbf, per, steps)):
+        n = len(ap)
+        np.testing.assert_array_equal(bp[off:off + n], ap, err_msg="scene %d positions" % k)
+        np.testing.assert_array_equal(bv[off:off + n], av, err_msg="scene %d velocities" % k)
+        off += n
+    assert off == len(bp)
+    mean, mx = b.density_error()
+    assert np.isfinite(mean) and mean < 0.5
+
+
+def test_batch_takes_exactly_all_particles(pbf, scenes):
+    sc, prm, pos, vel, _ = scenes.batched_scenes(n_scenes=3, n_min=512, n_max=1024, seed=2)
+    b = pbf.PBFSolver()
+    b.initialize_batch(sc, prm)
+    with pytest.raises(pbf.OutOfRange):
+        b.set_particles(pos[:-1], vel[:-1])
+    b.set_particles(pos, vel)
+    b.step()
+    # Back to one scene on the same handle.
+    p, v, lo, hi, q = scenes.dam_break(8, 8, 8, (0.8, 0.8, 0.8))[:5]
+    b.initialize(len(p), lo, hi, q)
+    assert b.scene_count() == 0
+    b.set_particles(p, v)
+    b.step()
+    assert np.isfinite(b.copy_positions_to_host()).all()
+
+
+def test_batch_one_launch_per_stage(pbf, scenes):
+    """A batch enqueues the same kernels per frame as one scene."""
+    sc, prm, pos, vel, per = scenes.batched_scenes(n_scenes=5, n_min=512, n_max=2048, seed=4)
+    b = pbf.PBFSolver()
+    b.initialize_batch(sc, prm)
+    b.set_particles(pos, vel)
+    b.step()
+    p, v, lo, hi, q = per[0]
+    a = pbf.PBFSolver()
+    a.initialize(len(p), lo, hi, q)
+    a.set_particles(p, v)
+    a.step()
+    assert b.kernels_per_frame() == a.kernels_per_frame()
