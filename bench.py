@@ -319,6 +319,91 @@ def batched(pkg, scenes, steps: int, warmup: int, per_scene_steps: int):
     }
 
 
+def adjoint_bench(pkg, scenes, steps: int, every: int, ndirs: int):
+    """Differentiable rollout: 65,536 particles (64x64x16 lattice), `steps`
+    steps with checkpoints every `every`; loss = mean squared distance of the
+    final positions to the initial lattice shifted +0.3 in x with
+    N(0, 0.01h) noise; gradients w.r.t. v0, rest density and XSPH c, checked
+    against FP64 central finite differences of the FP64 restatement."""
+    from oracle import oracle as O
+    nx, ny, nz = 64, 64, 16
+    S = scenes.SPACING
+    box = (2 * nx * S, 1.5 * ny * S, 2 * nz * S)
+    pos, vel, mn, mx, prm, _ = scenes.dam_break(nx, ny, nz, box)
+    prm.vorticityStrength = 0.0
+    n = len(pos)
+    rng = np.random.default_rng(5)
+    target = pos[:, :3].astype(np.float64) + np.array([0.3, 0.0, 0.0])
+    target += rng.normal(0.0, 0.01 * scenes.H, target.shape)
+
+    a = pkg.PBFAdjoint()
+    a.initialize(n, mn, mx, prm, max_neighbors=128, checkpoint_every=every)
+    a.forward(pos, vel, steps)  # warm-up
+    cuda_sync()
+    t0 = time.perf_counter()
+    x, v = a.forward(pos, vel, steps)
+    cuda_sync()
+    t_fwd = time.perf_counter() - t0
+    d = x[:, :3].astype(np.float64) - target
+    gx = np.zeros((n, 4), np.float32)
+    gx[:, :3] = (2.0 / n) * d
+    t0 = time.perf_counter()
+    gx0, gv0, gr, gc = a.backward(gx, np.zeros_like(gx))
+    cuda_sync()
+    t_bwd = time.perf_counter() - t0
+    a.close()
+
+    s = pkg.PBFSolver()
+    s.initialize(n, mn, mx, prm)
+    s.set_particles(pos, vel)
+    s.run(3)
+    ms_solver = s.time_frames(steps)
+    s.close()
+
+    p = prm.as_dict()
+
+    def loss64(v0=vel, q=p):
+        xx, _ = O.diff_rollout(pos, v0, q, mn, mx, steps)
+        return float(((xx - target) ** 2).sum() / n)
+
+    e = 2.0 ** -16
+    errs = []
+    for k in range(ndirs):
+        dv = rng.standard_normal((n, 3))
+        vp, vm = vel.copy(), vel.copy()
+        vp[:, :3] += (e * dv).astype(np.float32)
+        vm[:, :3] -= (e * dv).astype(np.float32)
+        dvf = (vp[:, :3].astype(np.float64) - vm[:, :3].astype(np.float64)) / (2 * e)
+        fd = (loss64(v0=vp) - loss64(v0=vm)) / (2 * e)
+        ad = float((gv0[:, :3].astype(np.float64) * dvf).sum())
+        errs.append(abs(ad - fd) / abs(fd))
+
+    def fd_param(name, h):
+        r0 = p[name]
+        hi, lo = float(np.float32(r0 + h)), float(np.float32(r0 - h))
+        return (loss64(q=dict(p, **{name: hi})) - loss64(q=dict(p, **{name: lo}))) / (hi - lo)
+
+    fr = fd_param("restDensity", 0.01)
+    fc = fd_param("xsphViscosity", p["xsphViscosity"] * 1e-3)
+    return {
+        "particles": n, "steps": steps, "checkpoint_every": every,
+        "forward_ms": 1000.0 * t_fwd, "backward_ms": 1000.0 * t_bwd,
+        "adjoint_over_forward": t_bwd / t_fwd,
+        "solver_forward_ms": ms_solver,
+        "adjoint_over_solver_forward": 1000.0 * t_bwd / ms_solver,
+        "loss": float((d * d).sum() / n),
+        "grad_check": {
+            "reference": "FP64 central differences of the FP64 restatement "
+                         "(oracle/pbf_diff_oracle.cpp), step 2^-16 along random v0 directions",
+            "directions": ndirs, "v0_rel_err": errs, "v0_max_rel_err": max(errs),
+            "rest_density": {"adjoint": gr, "fd": fr, "rel_err": abs(gr - fr) / abs(fr)},
+            "xsph": {"adjoint": gc, "fd": fc, "rel_err": abs(gc - fc) / abs(fc)},
+        },
+        "workload": "64x64x16 dam-break lattice (spacing 0.5h) in a 6.4x4.8x1.6 box, "
+                    "vorticity off, other parameters as the 1M dam break",
+    }
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
@@ -359,6 +444,9 @@ def main():
     ap.add_argument("--no-reference-cuda", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-steps", type=int, default=60)
+    ap.add_argument("--adjoint-directions", type=int, default=8)
     ap.add_argument("--batched-steps", type=int, default=120)
     ap.add_argument("--per-scene-steps", type=int, default=20)
     ap.add_argument("--max-neighbors", type=int, default=256,
@@ -489,6 +577,9 @@ def main():
         if world == 1 and not args.no_batched:
             line["batched"] = batched(pkg, scenes, args.batched_steps, args.warmup,
                                       args.per_scene_steps)
+        if world == 1 and not args.no_adjoint:
+            line["adjoint"] = adjoint_bench(pkg, scenes, args.adjoint_steps, 10,
+                                            args.adjoint_directions)
         if not args.no_cpu_baseline and world == 1:
             budget = float(os.environ.get("PBF_CPU_SECONDS", "20"))
             line["cpu_baseline"] = cpu_baseline(scene, seconds_budget=budget)

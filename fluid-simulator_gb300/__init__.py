@@ -189,6 +189,14 @@ def _declare(L):
         "pbf_batch_initialize": ([_vp, C.POINTER(_Scene), C.c_int, C.POINTER(_Params), C.c_int],
                                  S),
         "pbf_batch_scene_count": ([_vp], C.c_int),
+        "pbf_adjoint_create": ([C.POINTER(_vp), C.c_int], S),
+        "pbf_adjoint_destroy": ([_vp], None),
+        "pbf_adjoint_last_error": ([_vp], C.c_char_p),
+        "pbf_adjoint_initialize": ([_vp, sz, F3, F3, C.POINTER(_Params), C.c_int, C.c_int], S),
+        "pbf_adjoint_set_physics": ([_vp, C.c_float, C.c_float], S),
+        "pbf_adjoint_forward": ([_vp, _vp, _vp, C.c_int, _vp, _vp], S),
+        "pbf_adjoint_backward": ([_vp, _vp, _vp, _vp, _vp, C.POINTER(C.c_double),
+                                  C.POINTER(C.c_double)], S),
         "pbf_set_stream": ([_vp, _vp], S),
         "pbf_density_error": ([_vp, C.POINTER(C.c_double), C.POINTER(C.c_double)], S),
         "pbf_copy_working_state": ([_vp, _vp, _vp, _vp, sz], S),
@@ -627,3 +635,90 @@ def integrate(positions, velocities, dt, gravity):
     _raise_global(load().pbf_integrate(_ptr(p), _ptr(xs), _ptr(v), p.shape[0], float(dt),
                                        _f3(gravity)))
     return xs, v
+
+
+class PBFAdjoint:
+    """Reverse-mode derivative of ``steps`` solver steps (pbf_adjoint_*).
+
+    ``forward`` runs the differentiated step (integration, density
+    constraint with s_corr and the container clamp, velocity update, XSPH,
+    container velocity response) from (x0, v0), keeping checkpoints;
+    ``backward`` takes dL/dx, dL/dv of that forward's final state and returns
+    dL/dx0, dL/dv0, dL/drestDensity and dL/dxsphViscosity.  Arrays are (n, 4)
+    float32 numpy arrays or contiguous CUDA tensors (anything with a
+    ``data_ptr``); outputs come back in the same kind as ``x0``.
+    """
+
+    def __init__(self, device: int = -1):
+        L = load()
+        h = _vp()
+        _raise_global(L.pbf_adjoint_create(C.byref(h), device))
+        self._h = h
+        self._L = L
+        self.n = 0
+
+    def close(self):
+        h = getattr(self, "_h", None)
+        if h:
+            self._L.pbf_adjoint_destroy(h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st: int):
+        if st != PBF_OK:
+            msg = self._L.pbf_adjoint_last_error(self._h).decode()
+            raise _STATUS_EXC.get(st, SolverRuntimeError)(msg)
+
+    def initialize(self, count: int, min_bounds, max_bounds, params: SimulationParams,
+                   max_neighbors: int = 128, checkpoint_every: int = 10):
+        self._params = params.to_struct()
+        self._check(self._L.pbf_adjoint_initialize(self._h, int(count), _f3(min_bounds),
+                                                   _f3(max_bounds), C.byref(self._params),
+                                                   int(max_neighbors), int(checkpoint_every)))
+        self.n = int(count)
+
+    def set_physics(self, rest_density: float, xsph_viscosity: float):
+        self._check(self._L.pbf_adjoint_set_physics(self._h, float(rest_density),
+                                                    float(xsph_viscosity)))
+
+    @staticmethod
+    def _arg(a, name, n):
+        if hasattr(a, "data_ptr"):
+            if tuple(a.shape) != (n, 4) or not a.is_contiguous():
+                raise InvalidArgument("%s must be a contiguous (n, 4) tensor" % name)
+            return a, a.data_ptr()
+        a = _f4_array(a, name)
+        if a.shape[0] != n:
+            raise InvalidArgument("%s must have %d rows" % (name, n))
+        return a, a.ctypes.data
+
+    def _like(self, ref):
+        if hasattr(ref, "data_ptr"):
+            import torch
+            t = torch.empty((self.n, 4), dtype=torch.float32, device=ref.device)
+            return t, t.data_ptr()
+        a = np.zeros((self.n, 4), np.float32)
+        return a, a.ctypes.data
+
+    def forward(self, x0, v0, steps: int):
+        x0, px = self._arg(x0, "x0", self.n)
+        v0, pv = self._arg(v0, "v0", self.n)
+        xo, pxo = self._like(x0)
+        vo, pvo = self._like(x0)
+        self._check(self._L.pbf_adjoint_forward(self._h, px, pv, int(steps), pxo, pvo))
+        return xo, vo
+
+    def backward(self, grad_x, grad_v):
+        gx, pgx = self._arg(grad_x, "grad_x", self.n)
+        gv, pgv = self._arg(grad_v, "grad_v", self.n)
+        gx0, p0 = self._like(gx)
+        gv0, p1 = self._like(gx)
+        gr, gc = C.c_double(), C.c_double()
+        self._check(self._L.pbf_adjoint_backward(self._h, pgx, pgv, p0, p1, C.byref(gr),
+                                                 C.byref(gc)))
+        return gx0, gv0, gr.value, gc.value

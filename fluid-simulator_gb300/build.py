@@ -20,7 +20,8 @@ BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_NAME = "libpbf103.so"
 LIB_PATH = os.path.join(BUILD_DIR, LIB_NAME)
 
-SOURCES = ["pbf_kernels.cu", "pbf_sort.cu", "pbf_solver.cu", "pbf_stages.cu", "pbf_noalloc.cu"]
+SOURCES = ["pbf_kernels.cu", "pbf_sort.cu", "pbf_solver.cu", "pbf_stages.cu", "pbf_noalloc.cu",
+           "pbf_adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",

@@ -4,6 +4,7 @@
 
 #include <cuda_runtime.h>
 
+#include <array>
 #include <cstddef>
 #include <stdexcept>
 #include <string>
@@ -21,6 +22,13 @@ struct Failure : std::runtime_error {
 };
 
 [[noreturn]] inline void fail(pbf_status s, const std::string& m) { throw Failure(s, m); }
+
+// Argument validation shared by the solver and the adjoint
+// (PBFSolver::initialize, src/pbf/pbf_solver.cu:45-79, and SpatialGrid
+// dimensions, src/pbf/spatial_grid.cu:10-64).
+bool finite3(pbf_float3 v);
+void validate_params(const pbf_params& p);
+std::array<int, 3> grid_dims_checked(pbf_float3 mn, pbf_float3 mx, float cell);
 
 inline void cuda_check(cudaError_t e) {
     if (e != cudaSuccess) fail(PBF_ERR_RUNTIME, cudaGetErrorString(e));

@@ -83,6 +83,11 @@ struct Marks {
     }
 };
 
+
+}  // namespace
+
+namespace pbf {
+
 bool finite3(pbf_float3 v) { return std::isfinite(v.x) && std::isfinite(v.y) && std::isfinite(v.z); }
 
 // Parameter validation of PBFSolver::initialize (src/pbf/pbf_solver.cu:45-79).
@@ -128,7 +133,7 @@ std::array<int, 3> grid_dims_checked(pbf_float3 mn, pbf_float3 mx, float cell) {
     return d;
 }
 
-}  // namespace
+}  // namespace pbf
 
 struct pbf_solver {
     int device = 0;

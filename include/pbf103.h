@@ -144,6 +144,36 @@ pbf_status pbf_batch_initialize(pbf_solver* s, const pbf_scene* scenes, int scen
 /* Scenes of a batched handle (0 after pbf_initialize). */
 int pbf_batch_scene_count(const pbf_solver* s);
 
+/* ---- reverse-mode derivative (no counterpart in the reference) ---------
+ * Gradients of a loss on the final state of `steps` steps with respect to
+ * the initial positions and velocities, restDensity (mass held fixed) and
+ * xsphViscosity.  The differentiated step is integration, the density
+ * constraint iterations with s_corr and the container clamp, the velocity
+ * update, XSPH and the container velocity response, over neighbour lists
+ * recorded by the forward (integer data, not differentiated); it runs the
+ * same arithmetic as PBFSolver::step in particle-id order (sums in another
+ * order, so it agrees with pbf_step to rounding).  One substep per step, no
+ * vorticity confinement, no sphere/box/plane colliders.  The forward keeps
+ * (x, v) every `checkpoint_every` steps; the backward recomputes each
+ * segment from its checkpoint.  State and gradient pointers may be host or
+ * device memory.  Gradient arrays are float4 with w ignored. */
+typedef struct pbf_adjoint pbf_adjoint;
+pbf_status pbf_adjoint_create(pbf_adjoint** out, int device);
+void pbf_adjoint_destroy(pbf_adjoint* a);
+const char* pbf_adjoint_last_error(const pbf_adjoint* a);
+pbf_status pbf_adjoint_initialize(pbf_adjoint* a, size_t count, pbf_float3 min_bounds,
+                                  pbf_float3 max_bounds, const pbf_params* params,
+                                  int max_neighbors, int checkpoint_every);
+/* Replace restDensity and xsphViscosity (drops the recorded forward). */
+pbf_status pbf_adjoint_set_physics(pbf_adjoint* a, float rest_density, float xsph_viscosity);
+pbf_status pbf_adjoint_forward(pbf_adjoint* a, const pbf_float4* x0, const pbf_float4* v0,
+                               int steps, pbf_float4* x_out, pbf_float4* v_out);
+/* grad_x / grad_v: dL/dx, dL/dv of the last forward's final state;
+ * returns dL/dx0, dL/dv0 and the two parameter derivatives. */
+pbf_status pbf_adjoint_backward(pbf_adjoint* a, const pbf_float4* grad_x, const pbf_float4* grad_v,
+                                pbf_float4* grad_x0, pbf_float4* grad_v0,
+                                double* grad_rest_density, double* grad_xsph);
+
 /* ---- streams, timing, diagnostics (no counterpart in the reference) ----- */
 /* Run subsequent work on `stream` (a cudaStream_t); NULL restores the solver's
  * own stream.  The solver still synchronises its own calls. */

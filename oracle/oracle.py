@@ -18,6 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libpbf_oracle.so")
 SRC = os.path.join(HERE, "pbf_oracle.cpp")
+SOURCES = [SRC, os.path.join(HERE, "pbf_diff_oracle.cpp")]
 
 ORC_OK, ORC_ERR_INVALID, ORC_ERR_LENGTH, ORC_ERR_OVERFLOW, ORC_ERR_NOT_CONVERGED = range(5)
 
@@ -25,13 +26,13 @@ ORC_OK, ORC_ERR_INVALID, ORC_ERR_LENGTH, ORC_ERR_OVERFLOW, ORC_ERR_NOT_CONVERGED
 def build(force: bool = False) -> str:
     """Compile the oracle with g++ (OpenMP, no FP contraction)."""
     os.makedirs(BUILD_DIR, exist_ok=True)
+    deps = SOURCES + [os.path.join(HERE, "pbf_oracle.h")]
     if (not force and os.path.exists(LIB_PATH)
-            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(SRC)
-            and os.path.getmtime(LIB_PATH) >= os.path.getmtime(os.path.join(HERE, "pbf_oracle.h"))):
+            and all(os.path.getmtime(LIB_PATH) >= os.path.getmtime(d) for d in deps)):
         return LIB_PATH
     tmp = LIB_PATH + ".tmp%d" % os.getpid()
     cmd = ["g++", "-O2", "-std=c++17", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared",
-           "-o", tmp, SRC]
+           "-o", tmp] + SOURCES
     subprocess.check_call(cmd)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
@@ -70,6 +71,9 @@ def lib():
     if _lib is None:
         _lib = C.CDLL(build())
         L = _lib
+        L.orc_diff_rollout.argtypes = [C.c_size_t, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int,
+                                       _vp, F3, F3, C.c_int, _vp, _vp, _vp, _vp]
+        L.orc_diff_rollout.restype = C.c_int
         L.orc_grid_dims.argtypes = [F3, F3, C.c_float, _i32p]
         L.orc_grid_dims.restype = C.c_int
         L.orc_grid_build.argtypes = [_vp, C.c_size_t, F3, C.c_float, _i32p, _vp, _vp, _vp, _vp]
@@ -526,3 +530,38 @@ class RefCudaSolver:
         if st not in (REF_OK, REF_OVERFLOW):
             self._ok(st)
         return nb, cnt, st_out.value, st == REF_OVERFLOW
+
+
+def diff_rollout(x0, v0, params: dict, lo, hi, steps: int, tx0=None, tv0=None, trho=None,
+                 tc=None):
+    """FP64 restatement of the differentiated step (pbf_diff_oracle.cpp).
+
+    x0, v0: (n, 4) float32.  Tangents: tx0 / tv0 of shape (k, n, 3), trho /
+    tc of shape (k,), k <= 12 directions.  Returns (x, v) as (n, 3) float64
+    and, with tangents, their derivatives (k, n, 3)."""
+    x0 = np.ascontiguousarray(x0, np.float32)
+    v0 = np.ascontiguousarray(v0, np.float32)
+    n = len(x0)
+    ks = [len(a) for a in (tx0, tv0, trho, tc) if a is not None]
+    k = max(ks) if ks else 0
+
+    def tan(a, shape):
+        if a is None:
+            return None
+        return np.ascontiguousarray(np.broadcast_to(np.asarray(a, np.float64), shape))
+
+    tx0 = tan(tx0, (k, n, 3))
+    tv0 = tan(tv0, (k, n, 3))
+    trho = tan(trho, (k,))
+    tc = tan(tc, (k,))
+    x = np.zeros((n, 3), np.float64)
+    v = np.zeros((n, 3), np.float64)
+    tx = np.zeros((k, n, 3), np.float64) if k else None
+    tv = np.zeros((k, n, 3), np.float64) if k else None
+    prm = params_struct(params)
+    st = lib().orc_diff_rollout(n, _p(x0), _p(v0), _p(tx0), _p(tv0), _p(trho), _p(tc), k,
+                                C.byref(prm), f3(lo), f3(hi), int(steps), _p(x), _p(v), _p(tx),
+                                _p(tv))
+    if st != ORC_OK:
+        raise RuntimeError("orc_diff_rollout failed with status %d" % st)
+    return (x, v, tx, tv) if k else (x, v)

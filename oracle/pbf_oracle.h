@@ -135,6 +135,18 @@ int orc_solver_copy_working(const orc_solver* s, orc_float4* pos, uint32_t* ids,
 /* Mean and max |rho/rho0 - 1| over the current working order and lists. */
 int orc_solver_density_error(const orc_solver* s, double* meanErr, double* maxErr);
 
+/* ---- FP64 forward-mode restatement of the differentiated step
+ * (pbf_diff_oracle.cpp): `steps` steps of integration, the density
+ * constraint with s_corr and the container clamp, velocity update, XSPH and
+ * container contacts, from (x0, v0), with ntan <= 12 tangent directions:
+ * tx0 / tv0 (ntan * n * 3 doubles or NULL) and trho / tc (ntan doubles or
+ * NULL) seed d(x0), d(v0), d(restDensity), d(xsphViscosity).  Outputs the
+ * final x, v (n * 3) and their tangents (ntan * n * 3, may be NULL). */
+int orc_diff_rollout(size_t n, const orc_float4* x0, const orc_float4* v0, const double* tx0,
+                     const double* tv0, const double* trho, const double* tc, int ntan,
+                     const orc_params* prm, orc_float3 lo, orc_float3 hi, int steps,
+                     double* x_out, double* v_out, double* tx_out, double* tv_out);
+
 #ifdef __cplusplus
 }
 #endif

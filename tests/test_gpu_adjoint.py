@@ -1,0 +1,127 @@
+"""Reverse-mode derivative of the PBF step on the GPU (pbf_adjoint_*).
+
+The adjoint's directional derivatives of L = mean |x_T - target|^2 are
+checked against the FP64 forward-mode gradient of the same steps
+(oracle/pbf_diff_oracle.cpp, pinned on the CPU against the FP64 oracle
+solver and its own central differences) and against FP64 central finite
+differences, along random directions in x0 and v0 and along rest density and
+XSPH strength.  Tolerance: 1e-3 relative, over trajectories that agree to
+FP32 rounding.
+"""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def scene(scenes, nx=16, ny=16, nz=8, seed=0):
+    box = (2 * nx * 0.05, ny * 0.05 * 1.5, 2 * nz * 0.05)
+    pos, vel, mn, mx, prm, _ = scenes.dam_break(nx, ny, nz, box, seed=seed)
+    prm.vorticityStrength = 0.0
+    prm.xsphViscosity = 2e-5
+    rng = np.random.default_rng(seed + 1)
+    target = pos[:, :3].astype(np.float64) + np.array([0.3, 0.0, 0.0])
+    target += rng.normal(0.0, 0.01 * 0.1, target.shape)
+    return pos, vel, mn, mx, prm, target
+
+
+def loss_grad(x, target):
+    n = len(target)
+    d = x[:, :3].astype(np.float64) - target
+    g = np.zeros((n, 4), np.float32)
+    g[:, :3] = (2.0 / n) * d
+    return float((d * d).sum() / n), g
+
+
+def adjoint_grads(pbf, pos, vel, mn, mx, prm, target, steps, every):
+    a = pbf.PBFAdjoint()
+    a.initialize(len(pos), mn, mx, prm, max_neighbors=128, checkpoint_every=every)
+    x, v = a.forward(pos, vel, steps)
+    L, gx = loss_grad(x, target)
+    gx0, gv0, gr, gc = a.backward(gx, np.zeros_like(gx))
+    a.close()
+    return x, L, gx0[:, :3].astype(np.float64), gv0[:, :3].astype(np.float64), gr, gc
+
+
+def test_taped_forward_follows_the_solver(pbf, scenes):
+    pos, vel, mn, mx, prm, _ = scene(scenes)
+    a = pbf.PBFAdjoint()
+    a.initialize(len(pos), mn, mx, prm, max_neighbors=128, checkpoint_every=3)
+    x, v = a.forward(pos, vel, 5)
+    s = pbf.PBFSolver()
+    s.initialize(len(pos), mn, mx, prm)
+    s.set_particles(pos, vel)
+    s.run(5)
+    np.testing.assert_allclose(x, s.copy_positions_to_host(), atol=2e-5, rtol=0)
+    np.testing.assert_allclose(v, s.copy_velocities_to_host(), atol=2e-3, rtol=0)
+
+
+def test_adjoint_matches_fp64_forward_mode_and_finite_differences(pbf, scenes, orc):
+    pos, vel, mn, mx, prm, target = scene(scenes)
+    steps, every = 6, 4  # two segments, the second shorter
+    x, L, gx0, gv0, gr, gc = adjoint_grads(pbf, pos, vel, mn, mx, prm, target, steps, every)
+    n = len(pos)
+    rng = np.random.default_rng(11)
+    dirs_v = rng.standard_normal((3, n, 3))
+    dirs_x = rng.standard_normal((2, n, 3)) * 1e-2
+    # Forward mode (FP64): 3 v0 directions, 2 x0 directions, rho0, c.
+    k = 7
+    tv = np.zeros((k, n, 3))
+    tx = np.zeros((k, n, 3))
+    tv[:3] = dirs_v
+    tx[3:5] = dirs_x
+    trho = np.zeros(k)
+    tc = np.zeros(k)
+    trho[5] = 1.0
+    tc[6] = 1.0
+    p = prm.as_dict()
+    x64, v64, txo, _ = orc.diff_rollout(pos, vel, p, mn, mx, steps, tx0=tx, tv0=tv, trho=trho,
+                                        tc=tc)
+    np.testing.assert_allclose(x[:, :3], x64, atol=5e-5, rtol=0)
+    d = (x64 - target) * (2.0 / n)
+    jvp = np.array([(d * txo[q]).sum() for q in range(k)])
+    adj = np.array([(gv0 * dirs_v[0]).sum(), (gv0 * dirs_v[1]).sum(), (gv0 * dirs_v[2]).sum(),
+                    (gx0 * dirs_x[0]).sum(), (gx0 * dirs_x[1]).sum(), gr, gc])
+    rel = np.abs(adj - jvp) / np.abs(jvp)
+    assert (rel <= 1e-3).all(), (adj, jvp, rel)
+
+    # FP64 central differences along the first v0 direction and rest density.
+    def loss64(v0=vel, q=p):
+        xx, _ = orc.diff_rollout(pos, v0, q, mn, mx, steps)
+        return float(((xx - target) ** 2).sum() / n)
+
+    e = 2.0 ** -16
+    vp, vm = vel.copy(), vel.copy()
+    vp[:, :3] += (e * dirs_v[0]).astype(np.float32)
+    vm[:, :3] -= (e * dirs_v[0]).astype(np.float32)
+    dvf = (vp[:, :3].astype(np.float64) - vm[:, :3].astype(np.float64)) / (2 * e)
+    fd_v = (loss64(v0=vp) - loss64(v0=vm)) / (2 * e)
+    adj_v = (gv0 * dvf).sum()
+    assert abs(adj_v - fd_v) <= 1e-3 * abs(fd_v), (adj_v, fd_v)
+    r0 = p["restDensity"]
+    hi, lo = float(np.float32(r0 + 0.01)), float(np.float32(r0 - 0.01))
+    fd_r = (loss64(q=dict(p, restDensity=hi)) - loss64(q=dict(p, restDensity=lo))) / (hi - lo)
+    assert abs(gr - fd_r) <= 1e-3 * abs(fd_r), (gr, fd_r)
+
+
+def test_autograd_function(pbf, scenes):
+    torch = pytest.importorskip("torch")
+    import importlib
+    ag = importlib.import_module("fluid_simulator_gb300.autograd")
+    pos, vel, mn, mx, prm, target = scene(scenes, 8, 8, 4)
+    a = pbf.PBFAdjoint()
+    a.initialize(len(pos), mn, mx, prm, max_neighbors=128, checkpoint_every=2)
+    dev = torch.device("cuda", 0)
+    x0 = torch.tensor(pos, device=dev)
+    v0 = torch.tensor(vel, device=dev, requires_grad=True)
+    rho = torch.tensor(float(prm.restDensity), dtype=torch.float64, requires_grad=True)
+    c = torch.tensor(float(prm.xsphViscosity), dtype=torch.float64, requires_grad=True)
+    x, v = ag.rollout(a, x0, v0, rho, c, 5)
+    t = torch.tensor(target, device=dev, dtype=torch.float64)
+    L = ((x[:, :3].double() - t) ** 2).sum() / len(pos)
+    L.backward()
+    x_np, L2, gx0, gv0, gr, gc = adjoint_grads(pbf, pos, vel, mn, mx, prm, target, 5, 2)
+    np.testing.assert_allclose(v0.grad[:, :3].cpu().numpy(), gv0, rtol=1e-5, atol=1e-9)
+    assert abs(rho.grad.item() - gr) <= 1e-6 * abs(gr)
+    assert abs(c.grad.item() - gc) <= 1e-6 * abs(gc)
