@@ -1,0 +1,192 @@
+"""Per-kernel profile of one PBF frame with Nsight Compute.
+
+The counterpart of the reference's ``benchmark/profile.py`` (nsys + ncu), with
+no disassembly step.  Two kinds of ncu runs, both with ``--clock-control
+none``:
+
+1. a launch list of one whole frame (``gpu__time_duration.sum`` only, a
+   single replay pass): launches, device time and share per kernel;
+2. for each of the ``--top`` kernels by time, its first launch in the frame
+   captured alone (``--launch-skip`` to it, ``--launch-count 1``) with DRAM
+   bytes, L2 hit rate, issue and occupancy counters: achieved HBM GB/s =
+   DRAM bytes / duration.
+
+Each ncu run first runs the same workload without ncu and stops if it fails.
+Usage (on a machine with a GPU and ncu):
+
+    python fluid-simulator_gb300/profile_report.py --scene dam_break_1m --warmup 2 \\
+        --out report.md
+
+Times under ncu are serialised and cold-cache: compare shares, not absolutes.
+"""
+
+from __future__ import annotations
+
+import argparse
+import csv
+import importlib
+import importlib.util
+import io
+import os
+import subprocess
+import sys
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+METRICS = [
+    "gpu__time_duration.sum",
+    "dram__bytes_read.sum",
+    "dram__bytes_write.sum",
+    "lts__t_sector_hit_rate.pct",
+    "smsp__issue_active.avg.pct_of_peak_sustained_active",
+    "sm__warps_active.avg.pct_of_peak_sustained_active",
+    "launch__registers_per_thread",
+]
+
+
+def load_pkg():
+    name = "fluid_simulator_gb300"
+    if name in sys.modules:
+        return sys.modules[name]
+    spec = importlib.util.spec_from_file_location(name, os.path.join(HERE, "__init__.py"),
+                                                  submodule_search_locations=[HERE])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def child(scene: str, warmup: int, frames: int):
+    """The profiled workload: set_particles, `warmup` frames, `frames` frames."""
+    pkg = load_pkg()
+    scenes = importlib.import_module("fluid_simulator_gb300.scenes")
+    pos, vel, mn, mx, prm, col = scenes.SCENES[scene]()
+    s = pkg.PBFSolver()
+    s.initialize(len(pos), mn, mx, prm)
+    for k, fn in (("spheres", s.set_spheres), ("boxes", s.set_boxes), ("planes", s.set_planes)):
+        if col.get(k):
+            fn(col[k])
+    s.set_particles(pos, vel)
+    s.run(warmup)
+    s.run(frames)
+    print("kernels_per_frame %d" % s.kernels_per_frame(), flush=True)
+
+
+def run(cmd, **kw):
+    r = subprocess.run(cmd, capture_output=True, text=True, **kw)
+    if r.returncode != 0:
+        sys.stderr.write(r.stdout[-4000:] + r.stderr[-4000:])
+        raise SystemExit("command failed (%d): %s" % (r.returncode, " ".join(cmd)))
+    return r.stdout
+
+
+def ncu_rows(path):
+    text = open(path).read()
+    start = text.find('"ID"')
+    rows = list(csv.DictReader(io.StringIO(text[start:])))
+    return [r for r in rows if r.get("Kernel Name")]
+
+
+SCALE = {"ns": 1e-9, "nsecond": 1e-9, "us": 1e-6, "usecond": 1e-6, "ms": 1e-3, "msecond": 1e-3,
+         "s": 1.0, "second": 1.0, "byte": 1.0, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9,
+         "KB": 1e3, "MB": 1e6, "GB": 1e9}
+
+
+def value(r):
+    """Metric value in base units (seconds, bytes) where the unit is a scale."""
+    v = float(r["Metric Value"].replace(",", ""))
+    return v * SCALE.get(r.get("Metric Unit", ""), 1.0)
+
+
+def short(name: str) -> str:
+    name = name.split("(")[0]
+    for pre in ("void ", "(anonymous namespace)::", "pbf::", "adj::"):
+        name = name.replace(pre, "")
+    return name.replace("unnamed>::", "").strip()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--scene", default="dam_break_1m")
+    ap.add_argument("--warmup", type=int, default=2)
+    ap.add_argument("--top", type=int, default=4)
+    ap.add_argument("--ncu", default="ncu")
+    ap.add_argument("--out", default=None)
+    ap.add_argument("--child", action="store_true")
+    args = ap.parse_args()
+    if args.child:
+        child(args.scene, args.warmup, 1)
+        return 0
+
+    me = [sys.executable, os.path.abspath(__file__), "--child", "--scene", args.scene,
+          "--warmup", str(args.warmup)]
+    out = run(me)  # plain run first: it must succeed before ncu sees it
+    kpf = int(out.split("kernels_per_frame")[1].split()[0])
+    before = 2 + args.warmup * kpf  # set_particles launches two kernels
+    tmp = tempfile.mkdtemp(prefix="pbf_prof_")
+    lst = os.path.join(tmp, "launches.csv")
+    cmd1 = [args.ncu, "--metrics", "gpu__time_duration.sum", "--clock-control", "none",
+            "--launch-skip", str(before), "--launch-count", str(kpf), "--csv", "--log-file",
+            lst] + me
+    run(cmd1)
+    agg = {}
+    rows = [r for r in ncu_rows(lst) if r["Metric Name"] == "gpu__time_duration.sum"]
+    for pos, r in enumerate(rows):
+        k = short(r["Kernel Name"])
+        sec = value(r)
+        a = agg.setdefault(k, [0, 0.0, pos])  # count, time, first launch in the frame
+        a[0] += 1
+        a[1] += sec
+    total = sum(a[1] for a in agg.values())
+    order = sorted(agg.items(), key=lambda kv: -kv[1][1])
+
+    detail = {}
+    cmds = [" ".join(cmd1)]
+    for k, (cnt, _, first) in order[: args.top]:
+        # Exactly one launch: the kernel's first launch of the profiled frame.
+        path = os.path.join(tmp, "k_%d.csv" % len(detail))
+        cmd = [args.ncu, "--metrics", ",".join(METRICS), "--clock-control", "none",
+               "--launch-skip", str(before + first), "--launch-count", "1", "--csv",
+               "--log-file", path] + me
+        run(me)
+        run(cmd)
+        cmds.append(" ".join(cmd))
+        vals = {}
+        for r in ncu_rows(path):
+            if short(r["Kernel Name"]) != k:
+                continue
+            vals[r["Metric Name"]] = value(r)
+        detail[k] = vals
+
+    lines = ["# Kernel profile: %s, one frame after %d warm-up frames" % (args.scene,
+                                                                         args.warmup), "",
+             "Commands:", ""]
+    lines += ["    " + c for c in cmds]
+    lines += ["", "| kernel | launches / frame | device us | share |", "|---|---|---|---|"]
+    for k, (cnt, sec, _) in order:
+        lines.append("| %s | %d | %.1f | %.1f%% |" % (k, cnt, sec * 1e6, 100.0 * sec / total))
+    lines += ["", "Top kernels, one launch each:", "",
+              "| kernel | us | DRAM read MB | DRAM write MB | HBM GB/s | L2 hit % | issue % | "
+              "warps % | regs |", "|---|---|---|---|---|---|---|---|---|"]
+    for k, v in detail.items():
+        if "gpu__time_duration.sum" not in v:
+            continue
+        sec = v["gpu__time_duration.sum"]
+        rd = v.get("dram__bytes_read.sum", 0.0)
+        wr = v.get("dram__bytes_write.sum", 0.0)
+        lines.append("| %s | %.1f | %.1f | %.1f | %.0f | %.1f | %.1f | %.1f | %d |" % (
+            k, sec * 1e6, rd / 1e6, wr / 1e6, (rd + wr) / sec / 1e9 if sec else 0.0,
+            v.get("lts__t_sector_hit_rate.pct", 0.0),
+            v.get("smsp__issue_active.avg.pct_of_peak_sustained_active", 0.0),
+            v.get("sm__warps_active.avg.pct_of_peak_sustained_active", 0.0),
+            int(v.get("launch__registers_per_thread", 0))))
+    text = "\n".join(lines) + "\n"
+    if args.out:
+        with open(args.out, "w") as f:
+            f.write(text)
+    print(text)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -255,8 +255,8 @@ struct Diff {
 template <int K>
 int run(size_t n, const orc_float4* x0, const orc_float4* v0, const double* tx0,
         const double* tv0, const double* trho, const double* tc, int ntan, const orc_params* prm,
-        orc_float3 lo, orc_float3 hi, int steps, double* x_out, double* v_out, double* tx_out,
-        double* tv_out) {
+        orc_float3 lo, orc_float3 hi, int steps, const orc_float4* states, double* x_out,
+        double* v_out, double* tx_out, double* tv_out) {
     Diff<K> s;
     s.n = n;
     s.p = *prm;
@@ -294,7 +294,23 @@ int run(size_t n, const orc_float4* x0, const orc_float4* v0, const double* tx0,
             }
         }
     }
-    for (int t = 0; t < steps; ++t) s.step();
+    for (int t = 0; t < steps; ++t) {
+        if (states && t > 0) {
+            // Linearise about a given trajectory: the values restart from its
+            // state at the start of step t, the tangents carry on.
+            const orc_float4* xs = states + size_t(t) * 2 * n;
+            const orc_float4* vs = xs + n;
+            for (size_t i = 0; i < n; ++i) {
+                s.x[i].x.v = xs[i].x;
+                s.x[i].y.v = xs[i].y;
+                s.x[i].z.v = xs[i].z;
+                s.v[i].x.v = vs[i].x;
+                s.v[i].y.v = vs[i].y;
+                s.v[i].z.v = vs[i].z;
+            }
+        }
+        s.step();
+    }
     for (size_t i = 0; i < n; ++i) {
         const D3<K>& a = s.x[i];
         const D3<K>& b = s.v[i];
@@ -326,16 +342,17 @@ int run(size_t n, const orc_float4* x0, const orc_float4* v0, const double* tx0,
 extern "C" int orc_diff_rollout(size_t n, const orc_float4* x0, const orc_float4* v0,
                                 const double* tx0, const double* tv0, const double* trho,
                                 const double* tc, int ntan, const orc_params* prm,
-                                orc_float3 lo, orc_float3 hi, int steps, double* x_out,
-                                double* v_out, double* tx_out, double* tv_out) {
+                                orc_float3 lo, orc_float3 hi, int steps,
+                                const orc_float4* states, double* x_out, double* v_out,
+                                double* tx_out, double* tv_out) {
     if (!prm || !x0 || !v0 || !x_out || !v_out || ntan < 0 || ntan > 12 || steps < 0)
         return ORC_ERR_INVALID;
     if (ntan == 0)
         return run<0>(n, x0, v0, nullptr, nullptr, nullptr, nullptr, 0, prm, lo, hi, steps,
-                      x_out, v_out, nullptr, nullptr);
+                      states, x_out, v_out, nullptr, nullptr);
     if (ntan <= 4)
-        return run<4>(n, x0, v0, tx0, tv0, trho, tc, ntan, prm, lo, hi, steps, x_out, v_out,
-                      tx_out, tv_out);
-    return run<12>(n, x0, v0, tx0, tv0, trho, tc, ntan, prm, lo, hi, steps, x_out, v_out, tx_out,
-                   tv_out);
+        return run<4>(n, x0, v0, tx0, tv0, trho, tc, ntan, prm, lo, hi, steps, states, x_out,
+                      v_out, tx_out, tv_out);
+    return run<12>(n, x0, v0, tx0, tv0, trho, tc, ntan, prm, lo, hi, steps, states, x_out, v_out,
+                   tx_out, tv_out);
 }

@@ -140,12 +140,17 @@ int orc_solver_density_error(const orc_solver* s, double* meanErr, double* maxEr
  * constraint with s_corr and the container clamp, velocity update, XSPH and
  * container contacts, from (x0, v0), with ntan <= 12 tangent directions:
  * tx0 / tv0 (ntan * n * 3 doubles or NULL) and trho / tc (ntan doubles or
- * NULL) seed d(x0), d(v0), d(restDensity), d(xsphViscosity).  Outputs the
- * final x, v (n * 3) and their tangents (ntan * n * 3, may be NULL). */
+ * NULL) seed d(x0), d(v0), d(restDensity), d(xsphViscosity).  With
+ * `states` (steps * 2 * n float4: x then v at the start of each step, or
+ * NULL) the values restart from that trajectory at every step while the
+ * tangents carry on: the derivative linearised about a given (for instance
+ * FP32) trajectory.  Outputs the final x, v (n * 3) and their tangents
+ * (ntan * n * 3, may be NULL). */
 int orc_diff_rollout(size_t n, const orc_float4* x0, const orc_float4* v0, const double* tx0,
                      const double* tv0, const double* trho, const double* tc, int ntan,
                      const orc_params* prm, orc_float3 lo, orc_float3 hi, int steps,
-                     double* x_out, double* v_out, double* tx_out, double* tv_out);
+                     const orc_float4* states, double* x_out, double* v_out, double* tx_out,
+                     double* tv_out);
 
 #ifdef __cplusplus
 }

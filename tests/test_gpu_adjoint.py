@@ -5,8 +5,14 @@ checked against the FP64 forward-mode gradient of the same steps
 (oracle/pbf_diff_oracle.cpp, pinned on the CPU against the FP64 oracle
 solver and its own central differences) and against FP64 central finite
 differences, along random directions in x0 and v0 and along rest density and
-XSPH strength.  Tolerance: 1e-3 relative, over trajectories that agree to
-FP32 rounding.
+XSPH strength.  Tolerance: 1e-3 relative.
+
+Over a few steps the FP32 and FP64 trajectories agree to rounding and both
+references apply.  Over longer horizons the collapsing dam is chaotic (the
+FP64 derivative itself grows by orders of magnitude and no longer matches
+FP64 central differences), so the long-horizon check linearises the FP64
+tangents about the GPU's own trajectory: the same derivative, evaluated on
+the same states.
 """
 
 import numpy as np
@@ -125,3 +131,41 @@ def test_autograd_function(pbf, scenes):
     np.testing.assert_allclose(v0.grad[:, :3].cpu().numpy(), gv0, rtol=1e-5, atol=1e-9)
     assert abs(rho.grad.item() - gr) <= 1e-6 * abs(gr)
     assert abs(c.grad.item() - gc) <= 1e-6 * abs(gc)
+
+
+def gpu_states(a, pos, vel, steps):
+    """(steps, 2, n, 4): x, v at the start of each step of the taped forward."""
+    out = np.zeros((steps, 2, len(pos), 4), np.float32)
+    x, v = pos, vel
+    for t in range(steps):
+        out[t, 0], out[t, 1] = x, v
+        x, v = a.forward(x, v, 1)
+    return out
+
+
+def test_adjoint_matches_fp64_tangents_along_its_trajectory(pbf, scenes, orc):
+    pos, vel, mn, mx, prm, target = scene(scenes)
+    steps, every = 20, 7  # three segments, the last shorter
+    n = len(pos)
+    a = pbf.PBFAdjoint()
+    a.initialize(n, mn, mx, prm, max_neighbors=128, checkpoint_every=every)
+    states = gpu_states(a, pos, vel, steps)
+    x, v = a.forward(pos, vel, steps)
+    d = x[:, :3].astype(np.float64) - target
+    gx = np.zeros((n, 4), np.float32)
+    gx[:, :3] = (2.0 / n) * d
+    gx0, gv0, gr, gc = a.backward(gx, np.zeros_like(gx))
+    rng = np.random.default_rng(13)
+    dirs = rng.standard_normal((3, n, 3))
+    k = 5
+    tv = np.zeros((k, n, 3))
+    tv[:3] = dirs
+    trho = np.array([0, 0, 0, 1.0, 0])
+    tc = np.array([0, 0, 0, 0, 1.0])
+    _, _, txo, _ = orc.diff_rollout(pos, vel, prm.as_dict(), mn, mx, steps, tv0=tv, trho=trho,
+                                    tc=tc, states=states)
+    jvp = np.array([(d * (2.0 / n) * txo[q]).sum() for q in range(k)])
+    g = gv0[:, :3].astype(np.float64)
+    adj = np.array([(g * dirs[0]).sum(), (g * dirs[1]).sum(), (g * dirs[2]).sum(), gr, gc])
+    rel = np.abs(adj - jvp) / np.abs(jvp)
+    assert (rel <= 1e-3).all(), (adj, jvp, rel)
