@@ -229,7 +229,7 @@ def cpu_baseline(scene, seconds_budget: float = 20.0, threads: int = 0):
                       "(FP32 C++/OpenMP restatement, %.1f s)" % (steps, len(pos), dt)}
 
 
-def reference_cuda(scene, steps: int, warmup: int):
+def reference_cuda(scene, steps: int, warmup: int, max_neighbors: int = 256):
     """The reference's own kernels (compiled from its sources, Release, sm_103a)
     driven with PBFSolver's host sequence, timed like its benchmark: steady
     clock around each step() (benchmark/pbf_benchmark.cu:121-137)."""
@@ -240,7 +240,7 @@ def reference_cuda(scene, steps: int, warmup: int):
                                "sources at build time)"}
     pos, vel, mn, mx, prm, col = scene
     r = O.RefCudaSolver()
-    r.initialize(len(pos), mn, mx, prm.as_dict())
+    r.initialize(len(pos), mn, mx, prm.as_dict(), max_neighbors)
     sp = [(*c, rr) for c, rr in col.get("spheres", [])]
     bx = [(*c, *e) for c, e in col.get("boxes", [])]
     r.set_colliders(np.asarray(sp, np.float32).reshape(-1, 4),
@@ -252,7 +252,7 @@ def reference_cuda(scene, steps: int, warmup: int):
     ms = r.time_steps(steps)
     r.close()
     return {"value": len(pos) * steps / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms / steps,
-            "steps": steps, "warmup": warmup,
+            "steps": steps, "warmup": warmup, "max_neighbors": max_neighbors,
             "method": "reference kernels compiled from its sources (-O3 -DNDEBUG, sm_103a), "
                       "PBFSolver host sequence and synchronisation, steady_clock around each "
                       "step()"}
@@ -620,7 +620,8 @@ def main():
             "density_error": {"mean": density[0], "max": density[1]},
         }
         if world == 1 and not args.no_reference_cuda:
-            line["reference_cuda"] = reference_cuda(scene, args.steps, args.warmup)
+            line["reference_cuda"] = reference_cuda(scene, args.steps, args.warmup,
+                                                    args.max_neighbors)
             if "value" in line["reference_cuda"]:
                 line["speedup_vs_reference_cuda"] = value / line["reference_cuda"]["value"]
         if world == 1 and not args.no_batched:

@@ -120,6 +120,21 @@ def main():
 
     me = [sys.executable, os.path.abspath(__file__), "--child", "--scene", args.scene,
           "--warmup", str(args.warmup)]
+    root = os.path.dirname(HERE)
+
+    def shown(cmd):
+        """The command as a user would type it from the repository root."""
+        out = []
+        for c in cmd:
+            if c == sys.executable:
+                c = "python"
+            elif os.path.isabs(c) and c.startswith(root + os.sep):
+                c = os.path.relpath(c, root)
+            elif os.path.isabs(c) and c.startswith(tempfile.gettempdir()):
+                c = "<tmp>/" + os.path.basename(c)
+            out.append(c)
+        return " ".join(out)
+
     out = run(me)  # plain run first: it must succeed before ncu sees it
     kpf = int(out.split("kernels_per_frame")[1].split()[0])
     before = 2 + args.warmup * kpf  # set_particles launches two kernels
@@ -141,7 +156,7 @@ def main():
     order = sorted(agg.items(), key=lambda kv: -kv[1][1])
 
     detail = {}
-    cmds = [" ".join(cmd1)]
+    cmds = [shown(cmd1)]
     for k, (cnt, _, first) in order[: args.top]:
         # Exactly one launch: the kernel's first launch of the profiled frame.
         path = os.path.join(tmp, "k_%d.csv" % len(detail))
@@ -150,7 +165,7 @@ def main():
                "--log-file", path] + me
         run(me)
         run(cmd)
-        cmds.append(" ".join(cmd))
+        cmds.append(shown(cmd))
         vals = {}
         for r in ncu_rows(path):
             if short(r["Kernel Name"]) != k:
@@ -160,7 +175,10 @@ def main():
 
     lines = ["# Kernel profile: %s, one frame after %d warm-up frames" % (args.scene,
                                                                          args.warmup), "",
-             "Commands:", ""]
+             "Generated by:", "",
+             "    python fluid-simulator_gb300/profile_report.py --scene %s --warmup %d --top %d"
+             % (args.scene, args.warmup, args.top), "",
+             "which runs (each after the same workload exited 0 without ncu):", ""]
     lines += ["    " + c for c in cmds]
     lines += ["", "| kernel | launches / frame | device us | share |", "|---|---|---|---|"]
     for k, (cnt, sec, _) in order:

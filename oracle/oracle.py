@@ -422,6 +422,7 @@ def ref_lib():
         L.ref_create.restype = _vp
         L.ref_destroy.argtypes = [_vp]
         L.ref_initialize.argtypes = [_vp, C.c_size_t, F3, F3, C.POINTER(Params)]
+        L.ref_initialize_ex.argtypes = [_vp, C.c_size_t, F3, F3, C.POINTER(Params), C.c_int]
         L.ref_set_colliders.argtypes = [_vp, _vp, C.c_size_t, _vp, C.c_size_t, _vp, C.c_size_t]
         L.ref_set_particles.argtypes = [_vp, _vp, _vp, C.c_size_t]
         L.ref_step.argtypes = [_vp]
@@ -464,10 +465,17 @@ class RefCudaSolver:
             raise RuntimeError("reference solver status %d: %s" % (
                 st, ref_lib().ref_last_error().decode()))
 
-    def initialize(self, max_particles, mn, mx, params: dict):
+    def initialize(self, max_particles, mn, mx, params: dict, max_neighbors: int = 256):
+        """max_neighbors other than the reference's 256: a raised-capacity
+        build (the kernels take the capacity as an argument)."""
         self._params = params_struct(params)
-        self._ok(ref_lib().ref_initialize(self._h, max_particles, f3(mn), f3(mx),
-                                          C.byref(self._params)))
+        self._max_nb = int(max_neighbors)
+        if self._max_nb == 256:
+            self._ok(ref_lib().ref_initialize(self._h, max_particles, f3(mn), f3(mx),
+                                              C.byref(self._params)))
+        else:
+            self._ok(ref_lib().ref_initialize_ex(self._h, max_particles, f3(mn), f3(mx),
+                                                 C.byref(self._params), self._max_nb))
 
     def set_colliders(self, spheres=(), boxes=(), planes=()):
         sp, bx, pl = colliders_arrays(spheres, boxes, planes)
@@ -523,7 +531,7 @@ class RefCudaSolver:
         sp = as_f4(sorted_pos)
         n = sp.shape[0]
         stride = ref_lib().ref_stride(self._h)
-        nb = np.zeros(stride * 256, np.uint32)
+        nb = np.zeros(stride * getattr(self, "_max_nb", 256), np.uint32)
         cnt = np.zeros(n, np.int32)
         st_out = C.c_size_t()
         st = ref_lib().ref_find_neighbors(self._h, _p(sp), n, _p(nb), _p(cnt), C.byref(st_out))

@@ -97,6 +97,7 @@ bool get(CUmodule m, const char* name, CUfunction* f) { return okd(cuModuleGetFu
 }  // namespace
 
 struct RefSolver {
+    int maxNbCap = kMaxNeighbors;  // kMaxNeighbors, or a raised capacity
     Kernels k;
     size_t maxParticles = 0, n = 0, stride = 0;
     RefParams prm{};
@@ -174,7 +175,7 @@ struct RefSolver {
     int search() {
         if (!ok(cudaMemset(overflow, 0, sizeof(int)))) return REF_ERR;
         float cell = prm.smoothingRadius, h = prm.smoothingRadius;
-        int maxNb = kMaxNeighbors;
+        int maxNb = maxNbCap;
         void* a[] = {&pred, &cs, &ce, &gridSize, &mn, &cell, &n, &h, &nbr, &cnt, &maxNb, &stride,
                      &overflow};
         if (!launch(k.search, n, a)) return REF_ERR;
@@ -214,7 +215,7 @@ struct RefSolver {
         if (n == 0) return REF_OK;
         const float sub = prm.dt / static_cast<float>(prm.substeps);
         int ni = static_cast<int>(n);
-        int maxNb = kMaxNeighbors;
+        int maxNb = maxNbCap;
         for (int s = 0; s < prm.substeps; ++s) {
             float3 g = prm.gravity;
             float dt = sub;
@@ -326,8 +327,11 @@ void ref_destroy(RefSolver* s) {
     delete s;
 }
 
-// PBFSolver::initialize allocations (validation is the product's job).
-int ref_initialize(RefSolver* s, size_t maxParticles, float3 mn, float3 mx, const RefParams* p) {
+// PBFSolver::initialize allocations (validation is the product's job), with
+// the list capacity `cap`.
+static int init_alloc(RefSolver* s, size_t maxParticles, float3 mn, float3 mx, const RefParams* p,
+                      int cap) {
+    s->maxNbCap = cap;
     s->release();
     s->maxParticles = maxParticles;
     s->prm = *p;
@@ -349,7 +353,7 @@ int ref_initialize(RefSolver* s, size_t maxParticles, float3 mn, float3 mx, cons
                 (s->rvel = dalloc<float4>(N)) && (s->rvin = dalloc<float4>(N)) &&
                 (s->delta = dalloc<float4>(N)) && (s->sid = dalloc<uint32_t>(N)) &&
                 (s->rsid = dalloc<uint32_t>(N)) &&
-                (s->nbr = dalloc<uint32_t>(s->stride * kMaxNeighbors)) &&
+                (s->nbr = dalloc<uint32_t>(s->stride * size_t(s->maxNbCap))) &&
                 (s->cnt = dalloc<int>(N)) && (s->overflow = dalloc<int>(1)) &&
                 (s->lam = dalloc<float>(N)) && (s->keys = dalloc<uint32_t>(N)) &&
                 (s->idx = dalloc<uint32_t>(N)) && (s->skeys = dalloc<uint32_t>(N)) &&
@@ -372,6 +376,22 @@ int ref_initialize(RefSolver* s, size_t maxParticles, float3 mn, float3 mx, cons
 }
 
 // spheres: (cx, cy, cz, r) x ns; boxes: 6 floats x nb; planes: 6 floats x np.
+int ref_initialize(RefSolver* s, size_t maxParticles, float3 mn, float3 mx, const RefParams* p) {
+    return init_alloc(s, maxParticles, mn, mx, p, kMaxNeighbors);
+}
+
+// The same with the neighbour capacity raised from kMaxNeighbors, as a patched
+// reference build would have it (src/pbf/pbf_solver.cu:12); the kernels take
+// the capacity as an argument.
+int ref_initialize_ex(RefSolver* s, size_t maxParticles, float3 mn, float3 mx, const RefParams* p,
+                      int maxNeighbors) {
+    if (maxNeighbors <= 0) {
+        g_err = "maxNeighbors must be positive";
+        return REF_ERR;
+    }
+    return init_alloc(s, maxParticles, mn, mx, p, maxNeighbors);
+}
+
 int ref_set_colliders(RefSolver* s, const float* sp, size_t ns, const float* bx, size_t nb,
                       const float* pl, size_t np) {
     for (void* p : {s->dSpheres, s->dBoxes, s->dPlanes})
@@ -459,7 +479,7 @@ int ref_find_neighbors(RefSolver* s, const float4* sp, size_t n, uint32_t* nbr, 
     s->n = keep;
     if (st == REF_ERR) return st;
     *stride_out = s->stride;
-    if (n && (!ok(cudaMemcpy(nbr, s->nbr, s->stride * kMaxNeighbors * 4, cudaMemcpyDeviceToHost)) ||
+    if (n && (!ok(cudaMemcpy(nbr, s->nbr, s->stride * size_t(s->maxNbCap) * 4, cudaMemcpyDeviceToHost)) ||
               !ok(cudaMemcpy(cnt, s->cnt, n * 4, cudaMemcpyDeviceToHost))))
         return REF_ERR;
     return st;
