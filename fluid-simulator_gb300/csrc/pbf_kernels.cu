@@ -332,12 +332,22 @@ k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
         // of the warp hit.  Same order as the list, so the same sums.
         // Neighbours are taken two at a time with FP32x2 arithmetic; the sums
         // stay in list order.
+        // The next pair's indices are loaded before this pair is gathered.
         LambdaAcc acc{c.k.c_poly6, 0.0f, 0.0f, 0.0f, 0.0f};
         int k = 0;
-#pragma unroll 2
+        uint32_t na = 0u, nb2 = 0u;
+        if (count >= 2) {
+            na = out[0];
+            nb2 = out[stride];
+        }
         for (; k + 2 <= count; k += 2) {
-            const float4 a = __ldg(&xs[out[static_cast<size_t>(k) * stride]]);
-            const float4 b = __ldg(&xs[out[static_cast<size_t>(k + 1) * stride]]);
+            const uint32_t ja = na, jb = nb2;
+            if (k + 4 <= count) {
+                na = out[static_cast<size_t>(k + 2) * stride];
+                nb2 = out[static_cast<size_t>(k + 3) * stride];
+            }
+            const float4 a = __ldg(&xs[ja]);
+            const float4 b = __ldg(&xs[jb]);
             const f32x2 dx = sub2(px, pack2(a.x, b.x));
             const f32x2 dy = sub2(py, pack2(a.y, b.y));
             const f32x2 dz = sub2(pz, pack2(a.z, b.z));
@@ -361,20 +371,33 @@ __device__ __forceinline__ bool count_ok(int count, int max_nb) {
     return count >= 0 && count <= max_nb;
 }
 
-// Walks a slot-major list in order: four indices, then the four gathers
-// (load(j)), are issued before any term is used, so dependent loads overlap.
-// Terms are handed over two at a time (use2(first, second)) for FP32x2
-// evaluation; a last odd neighbour goes to use1.  List order is kept.
+// Walks a slot-major list in order, four neighbours at a time: their four
+// gathers (load(j)) are issued before any term is used.  Terms are handed
+// over two at a time (use2(first, second)) for FP32x2 evaluation; a last odd
+// neighbour goes to use1.  List order is kept.
 template <class T, class Load, class Use2, class Use1>
 __device__ __forceinline__ void for_each_neighbor_pair(const uint32_t* __restrict__ row,
                                                        size_t stride, int count, Load load,
                                                        Use2 use2, Use1 use1) {
+    // The indices of the next four neighbours are loaded while the current
+    // four are gathered and used, so the list read (from DRAM) overlaps the
+    // dependent gathers instead of preceding them.
     int k = 0;
+    uint32_t jn[4];
+    if (count >= 4) {
+#pragma unroll
+        for (int b = 0; b < 4; ++b) jn[b] = __ldg(&row[static_cast<size_t>(b) * stride]);
+    }
     for (; k + 4 <= count; k += 4) {
         uint32_t j[4];
-        T v[4];
 #pragma unroll
-        for (int b = 0; b < 4; ++b) j[b] = __ldg(&row[static_cast<size_t>(k + b) * stride]);
+        for (int b = 0; b < 4; ++b) j[b] = jn[b];
+        if (k + 8 <= count) {
+#pragma unroll
+            for (int b = 0; b < 4; ++b)
+                jn[b] = __ldg(&row[static_cast<size_t>(k + 4 + b) * stride]);
+        }
+        T v[4];
 #pragma unroll
         for (int b = 0; b < 4; ++b) v[b] = load(j[b]);
         use2(v[0], v[1]);
