@@ -180,7 +180,8 @@ def allreduce_max(dist, v: float) -> float:
     if dist is None:
         return v
     import torch
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -269,6 +270,8 @@ def batched(pkg, scenes, steps: int, warmup: int, per_scene_steps: int):
     b.initialize_batch(sc, prm)
     b.set_particles(pos, vel)
     b.run(warmup)
+    tuned = b.autotune(2)
+    b.run(1)
     with Clocks(0) as clk:
         ms = b.time_frames(steps)
     kernels = b.kernels_per_frame()
@@ -307,7 +310,7 @@ def batched(pkg, scenes, steps: int, warmup: int, per_scene_steps: int):
     return {
         "scenes": len(sc), "particles": n, "steps": steps, "warmup": warmup,
         "value": value, "unit": UNIT, "ms_per_step": ms / steps, "kernels_per_step": kernels,
-        "gpu_launches": kernels * steps, "clocks": clk.summary(),
+        "gpu_launches": kernels * steps, "clocks": clk.summary(), "block_sizes": tuned,
         "density_error": {"mean": density[0], "max": density[1]},
         "per_scene_launches": {
             "value": one, "ms_per_step": 1000.0 * t_one / per_scene_steps,
@@ -491,6 +494,8 @@ def main():
     ap.add_argument("--no-reference-cuda", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default 256-thread blocks")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--adjoint-steps", type=int, default=60)
     ap.add_argument("--adjoint-directions", type=int, default=8)
@@ -519,6 +524,8 @@ def main():
             fn(col[k])
     s.set_particles(pos, vel)
     s.run(args.warmup)
+    tuned = s.autotune(2) if not args.no_autotune else s.block_sizes()
+    s.run(1)
     kernels = s.kernels_per_frame()
 
     # ---- device-timed value -------------------------------------------------
@@ -598,7 +605,8 @@ def main():
                        "substeps": prm.substeps, "parallelism": "replicas" if world > 1 else
                        "single GPU", "l2": "step working set ~250 MB > 129 MB L2 (no flush)",
                        "timing": "CUDA events around %d graph-replayed steps on the solver "
-                                 "stream" % args.steps},
+                                 "stream" % args.steps,
+                       "block_sizes": tuned},
             "clocks": clk.summary(),
             "e2e": {"value": e2e_value, "unit": UNIT,
                     "h2d_bytes_per_step": int(2 * 16 * n), "d2h_bytes_per_step": int(2 * 16 * n),

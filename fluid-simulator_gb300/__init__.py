@@ -189,6 +189,8 @@ def _declare(L):
         "pbf_batch_initialize": ([_vp, C.POINTER(_Scene), C.c_int, C.POINTER(_Params), C.c_int],
                                  S),
         "pbf_batch_scene_count": ([_vp], C.c_int),
+        "pbf_autotune": ([_vp, C.c_int], S),
+        "pbf_block_sizes": ([_vp, C.POINTER(C.c_int), C.c_int], S),
         "pbf_adjoint_create": ([C.POINTER(_vp), C.c_int], S),
         "pbf_adjoint_destroy": ([_vp], None),
         "pbf_adjoint_last_error": ([_vp], C.c_char_p),
@@ -362,6 +364,19 @@ class PBFSolver:
 
     def scene_count(self) -> int:
         return int(self._L.pbf_batch_scene_count(self._h))
+
+    TUNED_KERNELS = ("search_lambda", "delta_apply", "search_final", "xsph", "vorticity",
+                     "confine")
+
+    def autotune(self, frames_per_trial: int = 2) -> dict:
+        """pbf_autotune: choose the neighbour kernels' block sizes; returns them."""
+        self._check(self._L.pbf_autotune(self._h, int(frames_per_trial)))
+        return self.block_sizes()
+
+    def block_sizes(self) -> dict:
+        out = (C.c_int * 6)()
+        self._check(self._L.pbf_block_sizes(self._h, out, 6))
+        return dict(zip(self.TUNED_KERNELS, list(out)))
 
     def set_particles(self, positions, velocities, count: Optional[int] = None):
         if positions is None or velocities is None:

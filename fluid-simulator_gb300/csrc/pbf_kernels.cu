@@ -246,7 +246,7 @@ __device__ __forceinline__ float lambda_finish(const StepConst& c, const LambdaA
 }
 
 template <bool LAMBDA, bool B>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kMaxTunedBlock)
 k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
          const float* __restrict__ sy, const float* __restrict__ sz, const int* __restrict__ first,
          StepConst c, int n, uint32_t* __restrict__ nbr, int* __restrict__ cnt,
@@ -493,7 +493,7 @@ __device__ __forceinline__ void delta_sum(const StepConst& c, const float4* __re
 // delta p + applyDeltaPosition + CollisionSystem::solve + next cell keys.
 // N: artificial-pressure exponent fixed at compile time (0 = read at run time).
 template <int N, bool B>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kMaxTunedBlock)
 k_delta_apply(const float4* __restrict__ xs, const uint32_t* __restrict__ nbr,
               const int* __restrict__ cnt, const float* __restrict__ lam, StepConst c, int n,
               float4* __restrict__ xs_out, uint32_t* __restrict__ keys_out,
@@ -583,7 +583,7 @@ __device__ __forceinline__ float4 xsph_one(const StepConst& c, const float4* __r
 }
 
 template <bool B>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kMaxTunedBlock)
 k_xsph(const float4* __restrict__ x, const float4* __restrict__ v,
        const uint32_t* __restrict__ nbr, const int* __restrict__ cnt, StepConst c, int n,
        float4* __restrict__ v_out, const float4* __restrict__ vin, bool resolve,
@@ -598,7 +598,7 @@ k_xsph(const float4* __restrict__ x, const float4* __restrict__ v,
 }
 
 // computeVorticity (pbf_solver_kernels.cu:268-315).
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kMaxTunedBlock)
 k_vorticity(const float4* __restrict__ x, const float4* __restrict__ v,
             const uint32_t* __restrict__ nbr, const int* __restrict__ cnt, StepConst c, int n,
             float4* __restrict__ omega, bool store_norm, const unsigned* __restrict__ status) {
@@ -704,7 +704,7 @@ __device__ __forceinline__ float4 confine_one(const StepConst& c, const float4* 
 }
 
 template <bool B>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kMaxTunedBlock)
 k_confine(const float4* __restrict__ x, const uint32_t* __restrict__ nbr,
           const int* __restrict__ cnt, const float4* __restrict__ om,
           const float4* __restrict__ v, StepConst c, int n, float4* __restrict__ v_out,
@@ -864,21 +864,24 @@ void launch_gather_first(const uint32_t* perm, const float4* xs_in, float4* xs_o
     launch_k(k_gather_first, blocks_for(threads), kBlock, st, perm, xs_in, xs_out, org_in, org_out,
              sx, sy, sz, n, skeys, static_cast<uint32_t>(cells), first, status);
 }
+inline int tuned_block(const StepConst& c, int k) { return c.blk[k] > 0 ? c.blk[k] : kBlock; }
+
 void launch_search(const float4* xs, const float* sx, const float* sy, const float* sz,
                    const int* first, const StepConst& c, int n, uint32_t* nbr, int* cnt, float* lam,
                    unsigned* status, bool with_lambda, cudaStream_t st) {
-    const unsigned g = blocks_for(n);
+    const int bs = tuned_block(c, with_lambda ? kTunedSearchLambda : kTunedSearch);
+    const unsigned g = blocks_for(n, bs);
     if (with_lambda && c.scenes)
-        launch_k(k_search<true, true>, g, kBlock, st, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
+        launch_k(k_search<true, true>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
                  status);
     else if (with_lambda)
-        launch_k(k_search<true, false>, g, kBlock, st, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
+        launch_k(k_search<true, false>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
                  status);
     else if (c.scenes)
-        launch_k(k_search<false, true>, g, kBlock, st, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
+        launch_k(k_search<false, true>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
                  status);
     else
-        launch_k(k_search<false, false>, g, kBlock, st, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
+        launch_k(k_search<false, false>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
                  status);
 }
 
@@ -886,9 +889,10 @@ template <bool B>
 void launch_delta_apply_b(const float4* xs, const uint32_t* nbr, const int* cnt, const float* lam,
                           const StepConst& c, int n, float4* xs_out, uint32_t* keys_out,
                           unsigned* status, cudaStream_t st) {
-    const unsigned g = blocks_for(n);
+    const int bs = tuned_block(c, kTunedDelta);
+    const unsigned g = blocks_for(n, bs);
 #define PBF_DELTA_CASE(N)                                                                        \
-    launch_k(k_delta_apply<N, B>, g, kBlock, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out, status)
+    launch_k(k_delta_apply<N, B>, g, bs, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out, status)
     switch (c.sc.k != 0.0f ? c.sc.n : 0) {
         case 1: PBF_DELTA_CASE(1); break;
         case 2: PBF_DELTA_CASE(2); break;
@@ -916,17 +920,19 @@ void launch_finalize(const uint32_t* org, const float4* x_old, const float4* vin
 void launch_xsph(const float4* x, const float4* v, const uint32_t* nbr, const int* cnt,
                  const StepConst& c, int n, float4* v_out, const float4* vin, bool resolve,
                  const unsigned* status, cudaStream_t st) {
+    const int bs = tuned_block(c, kTunedXsph);
     if (c.scenes)
-        launch_k(k_xsph<true>, blocks_for(n), kBlock, st, x, v, nbr, cnt, c, n, v_out, vin, resolve,
-                 status);
+        launch_k(k_xsph<true>, blocks_for(n, bs), bs, st, x, v, nbr, cnt, c, n, v_out, vin,
+                 resolve, status);
     else
-        launch_k(k_xsph<false>, blocks_for(n), kBlock, st, x, v, nbr, cnt, c, n, v_out, vin,
+        launch_k(k_xsph<false>, blocks_for(n, bs), bs, st, x, v, nbr, cnt, c, n, v_out, vin,
                  resolve, status);
 }
 void launch_vorticity(const float4* x, const float4* v, const uint32_t* nbr, const int* cnt,
                       const StepConst& c, int n, float4* omega, bool store_norm,
                       const unsigned* status, cudaStream_t st) {
-    launch_k(k_vorticity, blocks_for(n), kBlock, st, x, v, nbr, cnt, c, n, omega, store_norm,
+    const int bs = tuned_block(c, kTunedVorticity);
+    launch_k(k_vorticity, blocks_for(n, bs), bs, st, x, v, nbr, cnt, c, n, omega, store_norm,
              status);
 }
 void launch_omega_norm(float4* omega, int n, cudaStream_t st) {
@@ -935,12 +941,13 @@ void launch_omega_norm(float4* omega, int n, cudaStream_t st) {
 void launch_confine(const float4* x, const uint32_t* nbr, const int* cnt, const float4* omega,
                     const float4* v, const StepConst& c, int n, float4* v_out,
                     const float4* vin, bool resolve, const unsigned* status, cudaStream_t st) {
+    const int bs = tuned_block(c, kTunedConfine);
     if (c.scenes)
-        launch_k(k_confine<true>, blocks_for(n), kBlock, st, x, nbr, cnt, omega, v, c, n, v_out,
+        launch_k(k_confine<true>, blocks_for(n, bs), bs, st, x, nbr, cnt, omega, v, c, n, v_out,
                  vin, resolve, status);
     else
-        launch_k(k_confine<false>, blocks_for(n), kBlock, st, x, nbr, cnt, omega, v, c, n, v_out,
-                 vin, resolve, status);
+        launch_k(k_confine<false>, blocks_for(n, bs), bs, st, x, nbr, cnt, omega, v, c, n,
+                 v_out, vin, resolve, status);
 }
 void launch_resolve(const float4* x, const float4* vin, float4* v, const StepConst& c, int n,
                     const unsigned* status, cudaStream_t st) {

@@ -37,7 +37,14 @@ struct StepConst {
     // (scenes occupy fixed contiguous slot ranges); null for one scene.
     const SceneConst* scenes;
     const uint16_t* sid;
+    // Threads per block of the tuned kernels (TunedKernel order); 0 = kBlock.
+    int blk[6];
 };
+
+// Kernels whose block size the solver's autotuner chooses.
+enum TunedKernel { kTunedSearchLambda, kTunedDelta, kTunedSearch, kTunedXsph, kTunedVorticity,
+                   kTunedConfine, kTunedCount };
+constexpr int kMaxTunedBlock = 512;
 
 constexpr int kBlock = 256;
 

@@ -161,6 +161,9 @@ struct pbf_solver {
     std::vector<size_t> scene_off;
     DeviceBuffer scene_tab, scene_id;
 
+    // Threads per block of the tuned kernels (0 = the default 256).
+    int tuned[kTunedCount] = {};
+
     // Device state.
     DeviceBuffer f4[kF4Pool];
     DeviceBuffer ids[2], org[2];
@@ -253,6 +256,7 @@ struct pbf_solver {
             c.scenes = scene_tab.as<SceneConst>();
             c.sid = scene_id.as<uint16_t>();
         }
+        for (int k = 0; k < kTunedCount; ++k) c.blk[k] = tuned[k];
         return c;
     }
 
@@ -462,6 +466,66 @@ struct pbf_solver {
             cuda_check(cudaEventElapsedTime(&t, marks.events[i], marks.events[i + 1]));
             ms[marks.stages[i]] += t;
             launches[marks.stages[i]] += 1;
+        }
+    }
+
+    // Block-size autotuner: for each tuned kernel, time its stage in profiled
+    // frames at 128, 256 and 512 threads per block and keep the fastest
+    // (coordinate descent, one kernel at a time; the other kernels keep their
+    // current sizes).  Block size changes no arithmetic, so results stay bit
+    // for bit the same.  The particle state is saved before and restored
+    // after, so tuning does not advance the simulation.
+    void autotune(int frames_per_trial) {
+        require_initialized("PBFSolver must be initialized before tuning");
+        if (n == 0) fail(PBF_ERR_LOGIC, "no particles to tune on");
+        if (frames_per_trial <= 0) fail(PBF_ERR_INVALID_ARGUMENT, "frames per trial must be positive");
+        use_device();
+        DeviceBuffer sx(n * sizeof(float4)), sv(n * sizeof(float4));
+        copy_out(false, sx.as<float4>(), n, true);
+        copy_out(true, sv.as<float4>(), n, true);
+        std::vector<float> ms(kStageCount);
+        std::vector<int> launches(kStageCount);
+        int saved[kTunedCount];
+        std::copy(tuned, tuned + kTunedCount, saved);
+        try {
+            tune_all(frames_per_trial, ms, launches, sx.as<float4>(), sv.as<float4>());
+        } catch (...) {
+            std::copy(saved, saved + kTunedCount, tuned);
+            clear_graphs();
+            set_particles(sx.as<float4>(), sv.as<float4>(), n, true);
+            throw;
+        }
+        clear_graphs();
+        set_particles(sx.as<float4>(), sv.as<float4>(), n, true);
+    }
+
+    // Every trial frame starts from the saved state (x0, v0), so the sizes are
+    // compared on the same work.
+    void tune_all(int frames_per_trial, std::vector<float>& ms, std::vector<int>& launches,
+                  const float4* x0, const float4* v0) {
+        static const int stage_of[kTunedCount] = {kStSearchLambda, kStDeltaApply, kStSearch,
+                                                  kStXsph, kStVorticity, kStConfine};
+        static const int sizes[3] = {128, 256, 512};
+        for (int k = 0; k < kTunedCount; ++k) {
+            int best = tuned[k] > 0 ? tuned[k] : kBlock;
+            float best_ms = -1.0f;
+            for (int b : sizes) {
+                tuned[k] = b;
+                clear_graphs();
+                float t = -1.0f;
+                for (int f = 0; f < frames_per_trial; ++f) {
+                    set_particles(x0, v0, n, true);
+                    profile_frame(ms.data(), launches.data());
+                    const float v = ms[stage_of[k]];
+                    if (launches[stage_of[k]] == 0) break;  // stage not in this frame
+                    t = t < 0.0f ? v : std::min(t, v);
+                }
+                if (t >= 0.0f && (best_ms < 0.0f || t < best_ms)) {
+                    best_ms = t;
+                    best = b;
+                }
+            }
+            tuned[k] = best;
         }
     }
 
@@ -976,6 +1040,20 @@ pbf_status pbf_batch_initialize(pbf_solver* s, const pbf_scene* scenes, int scen
 }
 
 int pbf_batch_scene_count(const pbf_solver* s) { return s ? s->nscenes : 0; }
+
+pbf_status pbf_autotune(pbf_solver* s, int frames_per_trial) {
+    PBF_GUARD(s, s->autotune(frames_per_trial));
+}
+
+pbf_status pbf_block_sizes(const pbf_solver* s, int* sizes, int count) {
+    if (!s || !sizes) {
+        pbf::set_global_error("solver handle and sizes must not be null");
+        return PBF_ERR_INVALID_ARGUMENT;
+    }
+    for (int k = 0; k < count && k < kTunedCount; ++k)
+        sizes[k] = s->tuned[k] > 0 ? s->tuned[k] : kBlock;
+    return PBF_OK;
+}
 
 pbf_status pbf_set_stream(pbf_solver* s, void* stream) {
     PBF_GUARD(s, {

@@ -144,6 +144,16 @@ pbf_status pbf_batch_initialize(pbf_solver* s, const pbf_scene* scenes, int scen
 /* Scenes of a batched handle (0 after pbf_initialize). */
 int pbf_batch_scene_count(const pbf_solver* s);
 
+/* Block-size autotuner (no counterpart in the reference): for the six
+ * neighbour kernels (walk + lambda, delta p, final walk, XSPH, vorticity,
+ * confinement), times each at 128, 256 and 512 threads per block in profiled
+ * frames (`frames_per_trial` per size) and keeps the fastest.  Results do not
+ * change (block size changes no arithmetic); the particle state is restored,
+ * so tuning does not advance the simulation.  Needs particles set. */
+pbf_status pbf_autotune(pbf_solver* s, int frames_per_trial);
+/* The block sizes in use, in the order above (count <= 6 entries). */
+pbf_status pbf_block_sizes(const pbf_solver* s, int* sizes, int count);
+
 /* ---- reverse-mode derivative (no counterpart in the reference) ---------
  * Gradients of a loss on the final state of `steps` steps with respect to
  * the initial positions and velocities, restDensity (mass held fixed) and

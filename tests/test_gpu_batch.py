@@ -73,3 +73,25 @@ def test_batch_one_launch_per_stage(pbf, scenes):
     a.set_particles(p, v)
     a.step()
     assert b.kernels_per_frame() == a.kernels_per_frame()
+
+
+def test_autotune_keeps_results_and_state(pbf, scenes):
+    """pbf_autotune picks block sizes among 128/256/512, leaves the particle
+    state where it was and changes no result bit."""
+    pos, vel, mn, mx, prm, _ = scenes.dam_break_16k()
+    a = pbf.PBFSolver()
+    a.initialize(len(pos), mn, mx, prm)
+    a.set_particles(pos, vel)
+    a.run(3)
+    x0, v0 = a.copy_positions_to_host(), a.copy_velocities_to_host()
+    sizes = a.autotune(1)
+    assert set(sizes.values()) <= {128, 256, 512}
+    np.testing.assert_array_equal(a.copy_positions_to_host(), x0)
+    np.testing.assert_array_equal(a.copy_velocities_to_host(), v0)
+    a.run(4)
+    b = pbf.PBFSolver()
+    b.initialize(len(pos), mn, mx, prm)
+    b.set_particles(x0, v0)
+    b.run(4)
+    np.testing.assert_array_equal(a.copy_positions_to_host(), b.copy_positions_to_host())
+    np.testing.assert_array_equal(a.copy_velocities_to_host(), b.copy_velocities_to_host())
