@@ -72,6 +72,26 @@ STAGE_BYTES = {
 # from one ncu capture of the 1M dam break at frame 150, the state the timed
 # region averages over (profiles/k_search_dam_break_1m_frame150.md).
 TRAFFIC_BYTES = {"search_lambda": 103.668736e6 + 165.316864e6}
+# Warp instructions per launch of the same capture (smsp__inst_executed.sum):
+# the walk is issue-bound, so its issue rate is the roofline that binds it.
+INST_PER_LAUNCH = {"search_lambda": 245930457.0}
+SMS, ISSUE_PER_SM_CLK = 152, 4
+
+
+def issue_roofline(kernel, ms_per_launch, clocks, scene):
+    """Warp instructions per second of the dominant kernel against the SMs'
+    issue peak (4 per SM per clock at the SM clock sampled while timing)."""
+    inst = INST_PER_LAUNCH.get(kernel) if scene == "dam_break_1m" else None
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+    if not inst or not mhz:
+        return None
+    achieved = inst / (ms_per_launch / 1000.0) / 1e9
+    peak = SMS * ISSUE_PER_SM_CLK * mhz * 1e6 / 1e9
+    return {"bound": "issue", "kernel": kernel, "achieved": achieved, "peak": peak,
+            "unit": "G warp-instructions/s", "frac": achieved / peak,
+            "inst_per_launch": inst,
+            "source": "smsp__inst_executed.sum of one ncu capture at frame 150 "
+                      "(profiles/k_search_dam_break_1m_frame150.md)"}
 
 
 def load_pkg():
@@ -533,6 +553,7 @@ def main():
     barrier(dist)
     with Clocks(local) as clk:
         ms = s.time_frames(args.steps)
+    clocks = clk.summary()
     cuda_sync()
     barrier(dist)
     ms_max = allreduce_max(dist, ms)
@@ -607,7 +628,7 @@ def main():
                        "timing": "CUDA events around %d graph-replayed steps on the solver "
                                  "stream" % args.steps,
                        "block_sizes": tuned},
-            "clocks": clk.summary(),
+            "clocks": clocks,
             "e2e": {"value": e2e_value, "unit": UNIT,
                     "h2d_bytes_per_step": int(2 * 16 * n), "d2h_bytes_per_step": int(2 * 16 * n),
                     "steps": args.e2e_steps,
@@ -622,6 +643,8 @@ def main():
                          "peak_source": peak_kind,
                          "algorithmic_bytes_per_launch": dom_bytes,
                          "ms_per_launch": stages[dom]["ms_per_launch"]},
+            "issue_roofline": issue_roofline(dom, stages[dom]["ms_per_launch"], clocks,
+                                             args.scene),
             "step_roofline": {"bytes_per_particle_step": balg, "achieved": step_achieved,
                               "peak": hbm, "unit": "GB/s", "frac": step_achieved / hbm},
             "stages": stages,
