@@ -60,7 +60,7 @@ STAGE_BYTES = {
     "gather_ranges": 46.0,            # R perm, R/W x*, R/W composed permutation, first[]
     "search_lambda": 24.0,            # R x*, W lambda, W count
     "delta_apply_collide": 56.0,      # R x*, R lambda, W x* + next hash
-    "search_final": 20.0,
+    "search_final": 20.0 + 48.0,     # walk + XSPH pass (R x*, v; W count, v)
     "finalize": 68.0,
     "xsph": 48.0,
     "vorticity": 48.0,

@@ -245,15 +245,13 @@ __device__ __forceinline__ float lambda_finish(const StepConst& c, const LambdaA
     return lambda_finish(c.mass, c.rho0, c.gs2, c.lambda_eps, a);
 }
 
-template <bool LAMBDA, bool B>
-__global__ void __launch_bounds__(kMaxTunedBlock)
-k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
-         const float* __restrict__ sy, const float* __restrict__ sz, const int* __restrict__ first,
-         StepConst c, int n, uint32_t* __restrict__ nbr, int* __restrict__ cnt,
-         float* __restrict__ lam, unsigned* __restrict__ status) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || fatal(status)) return;
-    const float4 pi = xs[i];
+// The neighbour walk of particle i (position pi): writes the list slot-major
+// at out[slot * stride] (at most max_nb entries) and returns the full count.
+template <bool B>
+__device__ __forceinline__ int walk(const StepConst& c, int i, float4 pi,
+                                    const float* __restrict__ sx, const float* __restrict__ sy,
+                                    const float* __restrict__ sz, const int* __restrict__ first,
+                                    uint32_t* __restrict__ out) {
     GridConst g;
     uint32_t base;
     grid_of<B>(c, i, g, base);
@@ -269,7 +267,6 @@ k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
     const uint32_t gxy = gx * static_cast<uint32_t>(g.gy);
     const float h2 = c.k.h2;
     const int max_nb = c.max_nb;
-    uint32_t* __restrict__ out = nbr + i;
     const size_t stride = c.stride;
     const f32x2 px = pack2(pi.x, pi.x), py = pack2(pi.y, pi.y), pz = pack2(pi.z, pi.z);
     int count = 0;
@@ -320,6 +317,23 @@ k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
             }
         }
     }
+    return count;
+}
+
+template <bool LAMBDA, bool B>
+__global__ void __launch_bounds__(kMaxTunedBlock)
+k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
+         const float* __restrict__ sy, const float* __restrict__ sz, const int* __restrict__ first,
+         StepConst c, int n, uint32_t* __restrict__ nbr, int* __restrict__ cnt,
+         float* __restrict__ lam, unsigned* __restrict__ status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || fatal(status)) return;
+    const float4 pi = xs[i];
+    uint32_t* __restrict__ out = nbr + i;
+    const int count = walk<B>(c, i, pi, sx, sy, sz, first, out);
+    const int max_nb = c.max_nb;
+    const size_t stride = c.stride;
+    const f32x2 px = pack2(pi.x, pi.x), py = pack2(pi.y, pi.y), pz = pack2(pi.z, pi.z);
     cnt[i] = count;
     if (count > max_nb) atomicOr(status, kStatusNeighborOverflow);
     if (LAMBDA) {
@@ -594,6 +608,30 @@ k_xsph(const float4* __restrict__ x, const float4* __restrict__ v,
     if (resolve)
         resolve_velocity(colliders_of<B>(c, i), c.particle_radius, c.restitution, c.friction,
                          x[i], vin[i], out);
+    v_out[i] = out;
+}
+
+// The final rebuild's walk with XSPH fused in: the list is written, then
+// applyXsphViscosity runs over it in a second pass (velocities v are the
+// updated ones, computed before this walk), with the velocity response when
+// no vorticity pass follows.
+template <bool B>
+__global__ void __launch_bounds__(kMaxTunedBlock)
+k_search_xsph(const float4* __restrict__ xs, const float* __restrict__ sx,
+              const float* __restrict__ sy, const float* __restrict__ sz,
+              const int* __restrict__ first, StepConst c, int n, uint32_t* __restrict__ nbr,
+              int* __restrict__ cnt, const float4* __restrict__ v, float4* __restrict__ v_out,
+              const float4* __restrict__ vin, bool resolve, unsigned* __restrict__ status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || fatal(status)) return;
+    const float4 pi = xs[i];
+    const int count = walk<B>(c, i, pi, sx, sy, sz, first, nbr + i);
+    cnt[i] = count;
+    if (count > c.max_nb) atomicOr(status, kStatusNeighborOverflow);
+    float4 out = xsph_one(c, xs, v, nbr, count, i, B ? scene_of(c, i).xsph_c : c.xsph_c);
+    if (resolve)
+        resolve_velocity(colliders_of<B>(c, i), c.particle_radius, c.restitution, c.friction,
+                         pi, vin[i], out);
     v_out[i] = out;
 }
 
@@ -883,6 +921,20 @@ void launch_search(const float4* xs, const float* sx, const float* sy, const flo
     else
         launch_k(k_search<false, false>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
                  status);
+}
+
+void launch_search_xsph(const float4* xs, const float* sx, const float* sy, const float* sz,
+                        const int* first, const StepConst& c, int n, uint32_t* nbr, int* cnt,
+                        const float4* v, float4* v_out, const float4* vin, bool resolve,
+                        unsigned* status, cudaStream_t st) {
+    const int bs = tuned_block(c, kTunedSearch);
+    const unsigned g = blocks_for(n, bs);
+    if (c.scenes)
+        launch_k(k_search_xsph<true>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr, cnt, v, v_out,
+                 vin, resolve, status);
+    else
+        launch_k(k_search_xsph<false>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr, cnt, v, v_out,
+                 vin, resolve, status);
 }
 
 template <bool B>

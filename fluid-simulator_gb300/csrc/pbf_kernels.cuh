@@ -87,6 +87,12 @@ void launch_gather_first(const uint32_t* perm, const float4* xs_in, float4* xs_o
 void launch_search(const float4* xs, const float* sx, const float* sy, const float* sz,
                    const int* first, const StepConst& c, int n, uint32_t* nbr, int* cnt, float* lam,
                    unsigned* status, bool with_lambda, cudaStream_t st);
+// The final walk with XSPH in a second pass over the new lists (v: updated
+// velocities; resolve: apply the velocity response against vin as well).
+void launch_search_xsph(const float4* xs, const float* sx, const float* sy, const float* sz,
+                        const int* first, const StepConst& c, int n, uint32_t* nbr, int* cnt,
+                        const float4* v, float4* v_out, const float4* vin, bool resolve,
+                        unsigned* status, cudaStream_t st);
 void launch_delta_apply(const float4* xs, const uint32_t* nbr, const int* cnt, const float* lam,
                         const StepConst& c, int n, float4* xs_out, uint32_t* keys_out,
                         unsigned* status, cudaStream_t st);

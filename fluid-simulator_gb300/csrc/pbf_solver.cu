@@ -339,13 +339,10 @@ struct pbf_solver {
                 give(cur);
                 cur = nxt;
             }
-            if (post) {
-                rebuild();
-                M(kStSearch);
-                launch_search(P(cur), soa.as<float>(), soa.as<float>() + soa_stride(),
-                              soa.as<float>() + 2 * soa_stride(), cell_first.as<int>(), c, N,
-                              nbr.as<uint32_t>(), cnt.as<int>(), nullptr, sp, false, st);
-            }
+            // The final rebuild, then the velocity update (it needs only the
+            // composed permutation), then the final walk: with XSPH on, the
+            // walk applies XSPH in a second pass over its new lists.
+            if (post) rebuild();
             const int vnew = take();
             const int vinnew = take();
             const int idnew = 1 - rid;
@@ -364,11 +361,18 @@ struct pbf_solver {
             const bool vort = prm.vorticityStrength != 0.0f;
             if (xsph) {
                 const int t = take();
-                M(kStXsph);
-                launch_xsph(P(rx), P(rv), nbr.as<uint32_t>(), cnt.as<int>(), c, N, P(t), P(vin2),
-                            !vort, sp, st);
+                M(kStSearch);
+                launch_search_xsph(P(rx), soa.as<float>(), soa.as<float>() + soa_stride(),
+                                   soa.as<float>() + 2 * soa_stride(), cell_first.as<int>(), c,
+                                   N, nbr.as<uint32_t>(), cnt.as<int>(), P(rv), P(t), P(vin2),
+                                   !vort, sp, st);
                 give(rv);
                 rv = t;
+            } else if (vort) {
+                M(kStSearch);
+                launch_search(P(rx), soa.as<float>(), soa.as<float>() + soa_stride(),
+                              soa.as<float>() + 2 * soa_stride(), cell_first.as<int>(), c, N,
+                              nbr.as<uint32_t>(), cnt.as<int>(), nullptr, sp, false, st);
             }
             if (vort) {
                 const int om = take();
