@@ -11,11 +11,13 @@
 //   k_delta_apply    delta p + apply + collision projection + next keys
 //                                                                 (pbf_solver_kernels.cu:108-193,
 //                                                                  collision_system.cu:133-172)
-// After the last iteration (pbf_solver.cu:260-323):
-//   k_search<false>  rebuilt lists for the velocity terms
+// After the last iteration (pbf_solver.cu:260-323), after the final rebuild:
 //   k_finalize       gather x, v_in, ids by the composite permutation + velocity update
-//   k_xsph, k_vorticity, k_confine   (pbf_solver_kernels.cu:213-385), collision
-//                    velocity response fused into the last of them
+//   k_search_xsph    rebuilt lists for the velocity terms + XSPH over them
+//                    (k_search<false> when XSPH is off)
+//   k_vorticity, k_confine   (pbf_solver_kernels.cu:268-385), collision velocity
+//                    response fused into the last velocity kernel
+//   k_xsph           XSPH alone (stage API)
 //
 // Every floating-point operation uses the explicit-rounding helpers of
 // pbf_math.cuh so the host oracle reproduces the step bit for bit.
