@@ -425,15 +425,29 @@ def adjoint_bench(pkg, scenes, steps: int, every: int, ndirs: int, fd_steps: int
         xx, _ = O.diff_rollout(pos, v0, q, mn, mx, fd_steps)
         return float(((xx - target) ** 2).sum() / n)
 
-    e = 2.0 ** -20
-    fd_err = []
-    for q in range(ndirs):
+    # Step 2^-24: the rollout is piecewise smooth (container clamps), and
+    # steps of 2^-20 and above cross kinks often enough to move central
+    # differences by up to 1e-2 from the FP64 forward-mode derivative.
+    e = 2.0 ** -24
+    gnorm = float(np.linalg.norm(gvF))
+    fd_dirs = list(dirs) + [gvF / gnorm]  # random directions, then the gradient's own
+    fd_adj, fd_val = [], []
+    for dq in fd_dirs:
         vp, vm = vel.copy(), vel.copy()
-        vp[:, :3] += (e * dirs[q]).astype(np.float32)
-        vm[:, :3] -= (e * dirs[q]).astype(np.float32)
+        vp[:, :3] += (e * dq).astype(np.float32)
+        vm[:, :3] -= (e * dq).astype(np.float32)
         dvf = (vp[:, :3].astype(np.float64) - vm[:, :3].astype(np.float64)) / (2 * e)
-        fd = (loss64(v0=vp) - loss64(v0=vm)) / (2 * e)
-        fd_err.append(abs((gvF * dvf).sum() - fd) / abs(fd))
+        fd_val.append((loss64(v0=vp) - loss64(v0=vm)) / (2 * e))
+        fd_adj.append(float((gvF * dvf).sum()))
+    fd_adj, fd_val = np.array(fd_adj), np.array(fd_val)
+    fd_err = (np.abs(fd_adj - fd_val) / np.abs(fd_val)).tolist()
+    # A random direction's derivative is a sum of 3n terms of random sign and
+    # cancels; over Gaussian directions r, E[(e.r)^2] = |e|^2, so this ratio
+    # estimates the relative error of the whole v0 gradient.
+    fd_grad_err = float(np.sqrt(((fd_adj[:ndirs] - fd_val[:ndirs]) ** 2).sum()
+                                / (fd_val[:ndirs] ** 2).sum()))
+    lin_grad_err = float(np.sqrt(((adj[:ndirs] - jvp[:ndirs]) ** 2).sum()
+                                 / (jvp[:ndirs] ** 2).sum()))
 
     def fd_param(name, h):
         r0 = p[name]
@@ -461,12 +475,16 @@ def adjoint_bench(pkg, scenes, steps: int, every: int, ndirs: int, fd_steps: int
                          "about the GPU trajectory, %d v0 directions + rest density + XSPH c"
                          % ndirs,
             "rel_err": lin_err.tolist(), "max_rel_err": float(lin_err.max()),
+            "v0_gradient_rel_err": lin_grad_err,
             "adjoint": adj.tolist(), "fp64": jvp.tolist()},
         "check_finite_differences": {
             "steps": fd_steps,
-            "reference": "FP64 central differences of the FP64 restatement, step 2^-20 along "
-                         "the same v0 directions; 0.01 in rest density, 1e-3 relative in c",
-            "v0_rel_err": fd_err, "v0_max_rel_err": max(fd_err),
+            "reference": "FP64 central differences of the FP64 restatement, step 2^-24 along "
+                         "the same v0 directions and along the adjoint's v0 gradient; 0.01 in "
+                         "rest density, 1e-3 relative in c",
+            "v0_rel_err": fd_err[:ndirs], "v0_max_rel_err": max(fd_err[:ndirs]),
+            "v0_along_gradient_rel_err": fd_err[ndirs],
+            "v0_gradient_rel_err": fd_grad_err,
             "rest_density": {"adjoint": grF, "fd": fr, "rel_err": abs(grF - fr) / abs(fr)},
             "xsph": {"adjoint": gcF, "fd": fc, "rel_err": abs(gcF - fc) / abs(fc)}},
         "workload": "64x64x16 dam-break lattice (spacing 0.5h) in a 6.4x4.8x1.6 box, "

@@ -16,17 +16,28 @@
 // gs = m / rho0, C_i = rho_i / rho0 - 1, rho_i = m (W(0) + sum_j W_ij),
 // G_i = sum_j grad W_ij, S2_i = sum_j |grad W_ij|^2.
 //
-// The neighbour lists of every iteration are recorded (integer data, not
-// differentiated) in particle-id order, built by the solver's own grid, sort
-// and search kernels; clamps and contact decisions are recorded the same way.
-// A list holds j iff it holds i for j (d2 is computed bit-identically from
-// both sides), and grad W is odd while its Hessian is even, so every
-// transposed (scatter) term of the adjoint is evaluated as a gather over the
-// particle's own list: no atomics, a deterministic result.
+// The forward is the solver's own step, kernel for kernel (a step of the
+// adjoint from particle-id order is bit for bit the solver's step): predict;
+// per iteration a stable sort of the cell keys, the gather into the new
+// order, the walk with lambda, delta p with the container projection; the
+// final sort and gather, the velocity update and the walk with XSPH; then the
+// contact response, written back in particle-id order.  The tape of a step
+// keeps every sort's permutation, each iteration's positions, lambdas and
+// neighbour lists (integer data, not differentiated), which components the
+// projection moved, and the velocities entering XSPH and the contacts.
 //
-// Checkpointing: the forward keeps (x, v) every K steps; the backward
-// recomputes each K-step segment from its checkpoint into a tape and runs the
-// segment's adjoint in reverse.
+// The adjoint of an iteration runs in that iteration's sorted order.  A list
+// holds j iff it holds i for j (d2 is computed bit-identically from both
+// sides), and grad W is odd while its Hessian is even, so every transposed
+// (scatter) term of the adjoint is evaluated as a gather over the particle's
+// own list; the forward's gathers through a permutation become stores
+// through the same permutation (each target written once).  No atomics: the
+// result is deterministic.
+//
+// Checkpointing: the forward keeps (x, v) every K steps, in particle-id
+// order; the backward recomputes each K-step segment from its checkpoint into
+// the tape and runs the segment's adjoint in reverse.  Forward, recompute and
+// adjoint segments run as CUDA graphs.
 #include "pbf_common.h"
 #include "pbf_kernels.cuh"
 
@@ -34,7 +45,9 @@
 #include <array>
 #include <cmath>
 #include <limits>
+#include <map>
 #include <string>
+#include <tuple>
 #include <vector>
 
 namespace pbf {
@@ -86,9 +99,11 @@ __device__ __forceinline__ PairTerms pair_terms(const StepConst& c, float3 r) {
             t.fpr = fp / rr;
         }
         if (c.sc.k != 0.0f && c.sc.n > 0 && c.sc.dq2 < c.sc.h2) {
+            // ratio^(3n - 1) = (ratio^3)^(n - 1) ratio^2.
             const float ratio = (c.sc.h2 - d2) * c.sc.inv_den;
-            t.sp = 3.0f * c.sc.k * static_cast<float>(c.sc.n) *
-                   powf(ratio, 3.0f * static_cast<float>(c.sc.n) - 1.0f) * c.sc.inv_den;
+            const float r2 = ratio * ratio;
+            t.sp = 3.0f * c.sc.k * static_cast<float>(c.sc.n) * ipow(r2 * ratio, c.sc.n - 1) *
+                   r2 * c.sc.inv_den;
         }
     }
     return t;
@@ -97,135 +112,17 @@ __device__ __forceinline__ float3 hess(const PairTerms& t, float3 r, float3 u) {
     return t.f * u + (t.fpr * dot3(r, u)) * r;
 }
 
-// ---- taped forward (particle-id order) -------------------------------------
-
-__global__ void k_integrate(const float4* __restrict__ x, const float4* __restrict__ v,
-                            StepConst c, int n, float4* __restrict__ v1, float4* __restrict__ p0) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float4 vv = v[i];
-    const float4 p = x[i];
-    vv.x = ffma(c.gravx, c.dt, vv.x);
-    vv.y = ffma(c.gravy, c.dt, vv.y);
-    vv.z = ffma(c.gravz, c.dt, vv.z);
-    v1[i] = vv;
-    p0[i] = make_float4(ffma(vv.x, c.dt, p.x), ffma(vv.y, c.dt, p.y), ffma(vv.z, c.dt, p.z), p.w);
+// The gather passes give each particle kLanes consecutive threads: lane l
+// takes list entries l, l + kLanes, ...; the partial sums are combined by a
+// fixed butterfly (deterministic), after which every lane holds the total.
+constexpr int kLanes = 4;
+__device__ __forceinline__ float lane_sum(float v) {
+#pragma unroll
+    for (int m = 1; m < kLanes; m <<= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
+    return v;
 }
-
-// Lists found in sorted order, rewritten in particle-id order.
-__global__ void k_map_lists(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ nbr_s,
-                            const int* __restrict__ cnt_s, int n, size_t stride, int max_nb,
-                            uint32_t* __restrict__ nbr, int* __restrict__ cnt) {
-    const int s = blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= n) return;
-    // After a failed search (status set, kernels returned early) perm and
-    // the lists may hold stale data: only ids below n are ever written.
-    const uint32_t o = perm[s];
-    if (o >= static_cast<uint32_t>(n)) return;
-    const int k = max(0, cnt_s[s]);
-    cnt[o] = k;
-    const int m = min(k, max_nb);
-    for (int q = 0; q < m; ++q) {
-        const uint32_t j = nbr_s[static_cast<size_t>(q) * stride + s];
-        const uint32_t id = j < static_cast<uint32_t>(n) ? perm[j] : o;
-        nbr[static_cast<size_t>(q) * stride + o] = id < static_cast<uint32_t>(n) ? id : o;
-    }
-}
-
-// computeLambda over a recorded list (the solver's lambda arithmetic).
-__global__ void k_lambda(const float4* __restrict__ p, const uint32_t* __restrict__ nbr,
-                         const int* __restrict__ cnt, StepConst c, int n, float* __restrict__ lam) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4 pi = p[i];
-    const int count = min(cnt[i], c.max_nb);
-    float wsum = c.k.c_poly6, s2 = 0.0f, gx = 0.0f, gy = 0.0f, gz = 0.0f;
-    for (int k = 0; k < count; ++k) {
-        const float4 pj = __ldg(&p[__ldg(&nbr[static_cast<size_t>(k) * c.stride + i])]);
-        const float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y), dz = fsub(pi.z, pj.z);
-        const float d2 = dist2(dx, dy, dz);
-        wsum = fadd(wsum, poly6(c.k, d2));
-        float ax, ay, az;
-        spiky(c.k, dx, dy, dz, d2, ax, ay, az);
-        s2 = ffma(az, az, ffma(ay, ay, ffma(ax, ax, s2)));
-        gx = fadd(gx, ax);
-        gy = fadd(gy, ay);
-        gz = fadd(gz, az);
-    }
-    const float rho = fmul(c.mass, wsum);
-    const float denom = ffma(c.gs2, fadd(s2, dist2(gx, gy, gz)), c.lambda_eps);
-    lam[i] = fdiv(-fsub(fdiv(rho, c.rho0), 1.0f), denom);
-}
-
-// delta p + apply + container clamp; q (before the clamp) is recorded.
-__global__ void k_delta(const float4* __restrict__ p, const float* __restrict__ lam,
-                        const uint32_t* __restrict__ nbr, const int* __restrict__ cnt, StepConst c,
-                        int n, float4* __restrict__ q_out, float4* __restrict__ p_out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4 pi = p[i];
-    const float li = lam[i];
-    const int count = min(cnt[i], c.max_nb);
-    float ax = 0.0f, ay = 0.0f, az = 0.0f;
-    for (int k = 0; k < count; ++k) {
-        const uint32_t j = __ldg(&nbr[static_cast<size_t>(k) * c.stride + i]);
-        const float4 pj = __ldg(&p[j]);
-        const float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y), dz = fsub(pi.z, pj.z);
-        const float d2 = dist2(dx, dy, dz);
-        float gx, gy, gz;
-        spiky(c.k, dx, dy, dz, d2, gx, gy, gz);
-        const float ls = fadd(fadd(li, __ldg(&lam[j])), scorr<0>(c.sc, d2));
-        ax = ffma(ls, gx, ax);
-        ay = ffma(ls, gy, ay);
-        az = ffma(ls, gz, az);
-    }
-    float qx = fadd(pi.x, fmul(c.gs, ax)), qy = fadd(pi.y, fmul(c.gs, ay)),
-          qz = fadd(pi.z, fmul(c.gs, az));
-    q_out[i] = make_float4(qx, qy, qz, pi.w);
-    project_container(c.col, c.particle_radius, qx, qy, qz);
-    p_out[i] = make_float4(qx, qy, qz, pi.w);
-}
-
-__global__ void k_velocity(const float4* __restrict__ pI, const float4* __restrict__ x,
-                           const float4* __restrict__ v1, StepConst c, int n,
-                           float4* __restrict__ v2) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4 q = pI[i], xo = x[i];
-    v2[i] = make_float4(fmul(fsub(q.x, xo.x), c.inv_dt), fmul(fsub(q.y, xo.y), c.inv_dt),
-                        fmul(fsub(q.z, xo.z), c.inv_dt), v1[i].w);
-}
-
-__global__ void k_xsph(const float4* __restrict__ pI, const float4* __restrict__ v2,
-                       const uint32_t* __restrict__ nbr, const int* __restrict__ cnt, StepConst c,
-                       int n, float4* __restrict__ v3) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4 pi = pI[i], vi = v2[i];
-    const int count = min(cnt[i], c.max_nb);
-    float cx = 0.0f, cy = 0.0f, cz = 0.0f;
-    for (int k = 0; k < count; ++k) {
-        const uint32_t j = __ldg(&nbr[static_cast<size_t>(k) * c.stride + i]);
-        const float4 pj = __ldg(&pI[j]), vj = __ldg(&v2[j]);
-        const float w = poly6(c.k, dist2(fsub(pi.x, pj.x), fsub(pi.y, pj.y), fsub(pi.z, pj.z)));
-        cx = ffma(fsub(vj.x, vi.x), w, cx);
-        cy = ffma(fsub(vj.y, vi.y), w, cy);
-        cz = ffma(fsub(vj.z, vi.z), w, cz);
-    }
-    v3[i] = make_float4(ffma(c.xsph_c, cx, vi.x), ffma(c.xsph_c, cy, vi.y),
-                        ffma(c.xsph_c, cz, vi.z), vi.w);
-}
-
-__global__ void k_respond(const float4* __restrict__ pI, const float4* __restrict__ v1,
-                          const float4* __restrict__ v3, StepConst c, int n,
-                          float4* __restrict__ v4, float4* __restrict__ x_out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    float4 v = v3[i];
-    const float4 p = pI[i];
-    resolve_velocity(c.col, c.particle_radius, c.restitution, c.friction, p, v1[i], v);
-    v4[i] = v;
-    x_out[i] = p;
+__device__ __forceinline__ float3 lane_sum(float3 v) {
+    return make_float3(lane_sum(v.x), lane_sum(v.y), lane_sum(v.z));
 }
 
 // ---- adjoint -----------------------------------------------------------------
@@ -269,16 +166,21 @@ __device__ __forceinline__ Walls replay_walls(const StepConst& c, float4 p, floa
     return w;
 }
 
-// gv4 -> gv3 (velocity before the contacts) and gv1 (incoming velocity).
-__global__ void k_respond_adj(const float4* __restrict__ pI, const float4* __restrict__ v1,
+// gv4 -> gv3 (velocity before the contacts, final sorted order) and the
+// gradient of the incoming velocity v1, stored in particle-id order
+// (vin_F[s] = v1[org[s]] in the forward).
+__global__ void k_respond_adj(const float4* __restrict__ pF, const float4* __restrict__ vinF,
                               const float4* __restrict__ v3, const float4* __restrict__ gv4,
-                              StepConst c, int n, float4* __restrict__ gv3,
-                              float4* __restrict__ gv1) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4 vin = v1[i];
-    const Walls w = replay_walls(c, pI[i], vin, v3[i]);
-    float g[3] = {gv4[i].x, gv4[i].y, gv4[i].z};
+                              const uint32_t* __restrict__ org, StepConst c, int n,
+                              float4* __restrict__ gv3, float4* __restrict__ gv1) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const uint32_t o = org[s];
+    if (o >= static_cast<uint32_t>(n)) return;  // only after a failed forward
+    const float4 vin = vinF[s];
+    const Walls w = replay_walls(c, pF[s], vin, v3[s]);
+    const float4 g4 = gv4[o];
+    float g[3] = {g4.x, g4.y, g4.z};
     float gin[3] = {0.0f, 0.0f, 0.0f};
     const float ts = 1.0f - c.friction;
     for (int k = w.m - 1; k >= 0; --k) {
@@ -291,31 +193,40 @@ __global__ void k_respond_adj(const float4* __restrict__ pI, const float4* __res
         for (int b = 0; b < 3; ++b)
             if (b != a) g[b] *= ts;
     }
-    gv3[i] = make_float4(g[0], g[1], g[2], 0.0f);
-    gv1[i] = make_float4(gin[0], gin[1], gin[2], 0.0f);
+    gv3[s] = make_float4(g[0], g[1], g[2], 0.0f);
+    gv1[o] = make_float4(gin[0], gin[1], gin[2], 0.0f);
 }
 
-// XSPH and velocity-update adjoint, plus the clamp of the last iteration:
+// The gradient of q where the projection moved no component, 0 elsewhere.
+__device__ __forceinline__ float4 unmoved(uint8_t m, float3 g) {
+    return make_float4((m & 1u) ? 0.0f : g.x, (m & 2u) ? 0.0f : g.y, (m & 4u) ? 0.0f : g.z, 0.0f);
+}
+
+// XSPH and velocity-update adjoint in the final sorted order, then the final
+// gather and the projection of the last iteration:
 //   gv2_i = gv3_i + c sum_j (gv3_j - gv3_i) W_ij
-//   gp_I  = gx'_i + gv2_i / dt + c sum_j ((gv3_i - gv3_j).(v2_j - v2_i)) grad W_ij
-//   gxs_i = -gv2_i / dt                       (x enters v2)
+//   gp_F  = gx'_i + gv2_i / dt + c sum_j ((gv3_i - gv3_j).(v2_j - v2_i)) grad W_ij
+//   gxs   = -gv2_i / dt at the particle's id        (x enters v2)
 //   dL/dc += gv3_i . sum_j (v2_j - v2_i) W_ij
-//   gq_{I-1} = gp_I where the clamp left q unchanged, 0 elsewhere.
-__global__ void k_xsph_adj(const float4* __restrict__ pI, const float4* __restrict__ v2,
+//   gq_{I-1} at slot rel[s] of the last iteration's order = gp_F where the
+//   projection left the component unchanged, 0 elsewhere.
+__global__ void k_xsph_adj(const float4* __restrict__ pF, const float4* __restrict__ v2,
                            const float4* __restrict__ gv3, const uint32_t* __restrict__ nbr,
                            const int* __restrict__ cnt, const float4* __restrict__ gx_next,
-                           const float4* __restrict__ q_last, StepConst c, int n,
+                           const uint32_t* __restrict__ org, const uint32_t* __restrict__ rel,
+                           const uint8_t* __restrict__ moved_last, StepConst c, int n,
                            float4* __restrict__ gxs, float4* __restrict__ gq,
                            double* __restrict__ acc_c) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4 pi4 = pI[i];
-    const float3 pi = f3(pi4), vi = f3(v2[i]), gi = f3(gv3[i]);
-    const int count = min(cnt[i], c.max_nb);
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = tid / kLanes, lane = tid % kLanes;
+    const bool live = i < n;
+    const int ii = live ? i : 0;
+    const float3 pi = f3(pF[ii]), vi = f3(v2[ii]), gi = f3(gv3[ii]);
+    const int count = live ? min(cnt[i], c.max_nb) : 0;
     float3 sg = make_float3(0.0f, 0.0f, 0.0f), sv = sg, pos = sg;
-    for (int k = 0; k < count; ++k) {
+    for (int k = lane; k < count; k += kLanes) {
         const uint32_t j = __ldg(&nbr[static_cast<size_t>(k) * c.stride + i]);
-        const float3 r = pi - f3(__ldg(&pI[j]));
+        const float3 r = pi - f3(__ldg(&pF[j]));
         const PairTerms t = pair_terms(c, r);
         const float3 dv = f3(__ldg(&v2[j])) - vi;
         const float3 gj = f3(__ldg(&gv3[j]));
@@ -323,13 +234,17 @@ __global__ void k_xsph_adj(const float4* __restrict__ pI, const float4* __restri
         sv = sv + t.w * dv;
         pos = pos + dot3(gi - gj, dv) * t.gw;
     }
+    sg = lane_sum(sg);
+    sv = lane_sum(sv);
+    pos = lane_sum(pos);
+    if (!live || lane != 0) return;
     const float3 gv2 = gi + c.xsph_c * sg;
     acc_c[i] += static_cast<double>(dot3(gi, sv));
-    const float3 gp = f3(gx_next[i]) + c.inv_dt * gv2 + c.xsph_c * pos;
-    gxs[i] = make_float4(-c.inv_dt * gv2.x, -c.inv_dt * gv2.y, -c.inv_dt * gv2.z, 0.0f);
-    const float4 q = q_last[i];
-    gq[i] = make_float4(q.x == pi4.x ? gp.x : 0.0f, q.y == pi4.y ? gp.y : 0.0f,
-                        q.z == pi4.z ? gp.z : 0.0f, 0.0f);
+    const uint32_t o = org[i], r = rel[i];
+    if (o >= static_cast<uint32_t>(n) || r >= static_cast<uint32_t>(n)) return;
+    const float3 gp = f3(gx_next[o]) + c.inv_dt * gv2 + c.xsph_c * pos;
+    gxs[o] = make_float4(-c.inv_dt * gv2.x, -c.inv_dt * gv2.y, -c.inv_dt * gv2.z, 0.0f);
+    gq[r] = unmoved(moved_last[r], gp);
 }
 
 // First gather pass of one iteration's adjoint (u_ij = gq_i - gq_j):
@@ -344,14 +259,16 @@ __global__ void k_iter_adj_a(const float4* __restrict__ p, const float* __restri
                              const int* __restrict__ cnt, StepConst c, int n,
                              float4* __restrict__ gpart, float4* __restrict__ aux,
                              float* __restrict__ aa, double* __restrict__ acc_rho0) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float3 pi = f3(p[i]), gqi = f3(gq[i]);
-    const float li = lam[i];
-    const int count = min(cnt[i], c.max_nb);
-    float wsum = c.k.c_poly6, s2 = 0.0f, glam = 0.0f;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = tid / kLanes, lane = tid % kLanes;
+    const bool live = i < n;
+    const int ii = live ? i : 0;
+    const float3 pi = f3(p[ii]), gqi = f3(gq[ii]);
+    const float li = lam[ii];
+    const int count = live ? min(cnt[i], c.max_nb) : 0;
+    float wsum = 0.0f, s2 = 0.0f, glam = 0.0f;
     float3 G = make_float3(0.0f, 0.0f, 0.0f), X = G, dpos = G;
-    for (int k = 0; k < count; ++k) {
+    for (int k = lane; k < count; k += kLanes) {
         const uint32_t j = __ldg(&nbr[static_cast<size_t>(k) * c.stride + i]);
         const float3 r = pi - f3(__ldg(&p[j]));
         const PairTerms t = pair_terms(c, r);
@@ -365,6 +282,13 @@ __global__ void k_iter_adj_a(const float4* __restrict__ p, const float* __restri
         glam += ug;
         dpos = dpos + coef * hess(t, r, u) + (2.0f * t.sp * ug) * r;
     }
+    wsum = lane_sum(wsum) + c.k.c_poly6;
+    s2 = lane_sum(s2);
+    glam = lane_sum(glam);
+    G = lane_sum(G);
+    X = lane_sum(X);
+    dpos = lane_sum(dpos);
+    if (!live || lane != 0) return;
     const float rho = c.mass * wsum;
     const float S = s2 + dot3(G, G);
     const float D = c.gs2 * S + c.lambda_eps;
@@ -384,25 +308,29 @@ __global__ void k_iter_adj_a(const float4* __restrict__ p, const float* __restri
 // Second gather pass: the lambda adjoint's position terms,
 //   gp_i = gpart_i + sum_j [(a_i + a_j) gradW_ij
 //                         + 2 gs^2 H_ij ((gD_i + gD_j) g_ij + gD_i G_i - gD_j G_j)],
-// then either the clamp of the previous iteration (gq_{k-1}) or, after the
-// first iteration, the integration adjoint (gx_t, gv_t).
+// then the transposed gather of the iteration (slot rel[s] of the previous
+// order): either the projection of the previous iteration (gq_{k-1}) or,
+// after the first iteration, the integration adjoint (gx_t, gv_t in
+// particle-id order).
 __global__ void k_iter_adj_b(const float4* __restrict__ p, const float4* __restrict__ aux,
                              const float* __restrict__ aa, const uint32_t* __restrict__ nbr,
                              const int* __restrict__ cnt, const float4* __restrict__ gpart,
-                             const float4* __restrict__ q_prev, const float4* __restrict__ gxs,
-                             const float4* __restrict__ gv1, StepConst c, int n,
-                             float4* __restrict__ gq_prev, float4* __restrict__ gx_t,
-                             float4* __restrict__ gv_t) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4 pi4 = p[i];
-    const float3 pi = f3(pi4);
-    const float4 ai4 = aux[i];
+                             const uint32_t* __restrict__ rel,
+                             const uint8_t* __restrict__ moved_prev,
+                             const float4* __restrict__ gxs, const float4* __restrict__ gv1,
+                             StepConst c, int n, float4* __restrict__ gq_prev,
+                             float4* __restrict__ gx_t, float4* __restrict__ gv_t) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = tid / kLanes, lane = tid % kLanes;
+    const bool live = i < n;
+    const int ii = live ? i : 0;
+    const float3 pi = f3(p[ii]);
+    const float4 ai4 = aux[ii];
     const float3 Gi = f3(ai4);
-    const float gDi = ai4.w, ai = aa[i];
-    const int count = min(cnt[i], c.max_nb);
+    const float gDi = ai4.w, ai = aa[ii];
+    const int count = live ? min(cnt[i], c.max_nb) : 0;
     float3 acc = make_float3(0.0f, 0.0f, 0.0f);
-    for (int k = 0; k < count; ++k) {
+    for (int k = lane; k < count; k += kLanes) {
         const uint32_t j = __ldg(&nbr[static_cast<size_t>(k) * c.stride + i]);
         const float3 r = pi - f3(__ldg(&p[j]));
         const PairTerms t = pair_terms(c, r);
@@ -411,21 +339,44 @@ __global__ void k_iter_adj_b(const float4* __restrict__ p, const float4* __restr
         const float3 w = (gDi + gDj) * t.g + gDi * Gi - gDj * f3(aj4);
         acc = acc + (ai + __ldg(&aa[j])) * t.gw + (2.0f * c.gs2) * hess(t, r, w);
     }
+    acc = lane_sum(acc);
+    if (!live || lane != 0) return;
     const float3 gp = f3(gpart[i]) + acc;
-    if (q_prev) {
-        const float4 q = q_prev[i];
-        gq_prev[i] = make_float4(q.x == pi4.x ? gp.x : 0.0f, q.y == pi4.y ? gp.y : 0.0f,
-                                 q.z == pi4.z ? gp.z : 0.0f, 0.0f);
+    const uint32_t r = rel[i];
+    if (r >= static_cast<uint32_t>(n)) return;  // only after a failed forward
+    if (moved_prev) {
+        gq_prev[r] = unmoved(moved_prev[r], gp);
     } else {
         // p0 = x + v1 dt, v1 = v + g dt.
-        const float4 gs = gxs[i], g1 = gv1[i];
-        gx_t[i] = make_float4(gs.x + gp.x, gs.y + gp.y, gs.z + gp.z, 0.0f);
-        gv_t[i] = make_float4(g1.x + c.dt * gp.x, g1.y + c.dt * gp.y, g1.z + c.dt * gp.z, 0.0f);
+        const float4 gs = gxs[r], g1 = gv1[r];
+        gx_t[r] = make_float4(gs.x + gp.x, gs.y + gp.y, gs.z + gp.z, 0.0f);
+        gv_t[r] = make_float4(g1.x + c.dt * gp.x, g1.y + c.dt * gp.y, g1.z + c.dt * gp.z, 0.0f);
     }
+}
+
+// Contact response of the forward (resolveVelocitiesKernel, the solver's
+// arithmetic), with positions and velocities stored back in particle-id order.
+__global__ void k_respond_out(const float4* __restrict__ pF, const float4* __restrict__ vinF,
+                              const float4* __restrict__ v3, const uint32_t* __restrict__ org,
+                              StepConst c, int n, float4* __restrict__ x_out,
+                              float4* __restrict__ v_out) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n) return;
+    const uint32_t o = org[s];
+    if (o >= static_cast<uint32_t>(n)) return;  // only after a failed forward
+    const float4 p = pF[s];
+    float4 v = v3[s];
+    resolve_velocity(c.col, c.particle_radius, c.restitution, c.friction, p, vinF[s], v);
+    x_out[o] = p;
+    v_out[o] = v;
 }
 
 constexpr int kB = 256;
 inline unsigned grid(int n) { return static_cast<unsigned>((n + kB - 1) / kB); }
+// Grid of the gather passes (kLanes threads per particle).
+inline unsigned grid_lanes(int n) {
+    return static_cast<unsigned>((static_cast<size_t>(n) * kLanes + kB - 1) / kB);
+}
 
 }  // namespace adj
 }  // namespace pbf
@@ -445,37 +396,64 @@ struct pbf_adjoint {
     StepConst c{};
     SortPlan plan{};
 
-    // Neighbour-list builder (sorted order) and its scratch.
-    DeviceBuffer keys, skeys, sidx, akeys, aidx, first, xsorted, org, soa, nbr_s, cnt_s, scratch,
-        status;
+    // Scratch of one step: keys, sort buffers, composed permutations, the
+    // cell table, component arrays and the predicted / projected positions.
+    DeviceBuffer keys, skeys, akeys, aidx, orgs, first, soa, xs0, vin, pn, scratch, status;
+    // Tape of one segment (`every` step slots), see the accessors below.
+    DeviceBuffer tf4, tu32, tlam, tnb, tcn, tmv;
+    // States in particle-id order: slot j holds (x, v) entering step j of a
+    // recomputed segment; the forward alternates between slots 0 and 1.
+    DeviceBuffer states;
     // Checkpoints (x, v) every `every` steps.
     DeviceBuffer ckpt;
-    // Tape of one segment: per step kF4 float4 arrays, I lambdas, I + 1 lists.
-    DeviceBuffer tape4, tapel, tapen, tapec;
-    // Work arrays.
-    DeviceBuffer xa, va, xb, vb, gx, gv, gxs, gv1, gv3, gq0, gq1, gpart, aux, aa, acc_r, acc_c;
+    // Adjoint work arrays.
+    DeviceBuffer gx, gv, gxs, gv1, gv3, gq0, gq1, gpart, aux, aa, acc_r, acc_c;
+    // Captured segments: (kind, length, parity) -> graph.
+    std::map<std::tuple<int, int, int>, cudaGraphExec_t> graphs;
 
     ~pbf_adjoint() {
+        clear_graphs();
         if (stream) cudaStreamDestroy(stream);
     }
 
-    int f4_slots() const { return 2 * iters + 5; }
-    size_t soa_stride() const { return (n + 1 + 63) / 64 * 64; }
-    // Tape slots of step t: 0 x, 1 v1, 2 + k p_k (k = 0..I), 3 + I + k q_k
-    // (k < I), 3 + 2I v2, 4 + 2I v3.
-    float4* T(int t, int slot) {
-        return tape4.as<float4>() + (static_cast<size_t>(t) * f4_slots() + slot) * n;
+    void clear_graphs() {
+        for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+        graphs.clear();
     }
-    float* L(int t, int k) { return tapel.as<float>() + (static_cast<size_t>(t) * iters + k) * n; }
+
+    // Tape of step slot t.  float4 arrays: P(t, k) positions of sort k in its
+    // order (k = 0..I; k = I is the final sort, i.e. the step's new
+    // positions), then v2 (entering XSPH), v1 in the final order (entering
+    // the contacts) and v3 (leaving XSPH).  uint32 arrays: REL(t, k) the
+    // permutation of sort k (its slot s takes slot REL[s] of the previous
+    // order; for k = 0 that order is particle-id order), and ORG(t) the
+    // composed permutation of the final order (slot -> particle id).
+    int f4_per_step() const { return iters + 4; }
+    int u32_per_step() const { return iters + 2; }
+    float4* P(int t, int k) {
+        return tf4.as<float4>() + (static_cast<size_t>(t) * f4_per_step() + k) * n;
+    }
+    float4* V2(int t) { return P(t, iters + 1); }
+    float4* VINF(int t) { return P(t, iters + 2); }
+    float4* V3(int t) { return P(t, iters + 3); }
+    uint32_t* REL(int t, int k) {
+        return tu32.as<uint32_t>() + (static_cast<size_t>(t) * u32_per_step() + k) * n;
+    }
+    uint32_t* ORG(int t) { return REL(t, iters + 1); }
+    float* LAM(int t, int k) { return tlam.as<float>() + (static_cast<size_t>(t) * iters + k) * n; }
+    uint8_t* MV(int t, int k) { return tmv.as<uint8_t>() + (static_cast<size_t>(t) * iters + k) * n; }
     uint32_t* NB(int t, int k) {
-        return tapen.as<uint32_t>() + (static_cast<size_t>(t) * (iters + 1) + k) * stride * max_nb;
+        return tnb.as<uint32_t>() + (static_cast<size_t>(t) * (iters + 1) + k) * stride * max_nb;
     }
-    int* CN(int t, int k) { return tapec.as<int>() + (static_cast<size_t>(t) * (iters + 1) + k) * n; }
+    int* CN(int t, int k) { return tcn.as<int>() + (static_cast<size_t>(t) * (iters + 1) + k) * n; }
+    float4* SX(int j) { return states.as<float4>() + static_cast<size_t>(2 * j) * n; }
+    float4* SV(int j) { return states.as<float4>() + static_cast<size_t>(2 * j + 1) * n; }
+    size_t soa_stride() const { return (n + 1 + 63) / 64 * 64; }
 
     void initialize(size_t count, pbf_float3 lo, pbf_float3 hi, const pbf_params& p, int maxnb,
                     int ckpt_every) {
         if (count == 0) fail(PBF_ERR_INVALID_ARGUMENT, "particle count must be greater than zero");
-        if (count > static_cast<size_t>(std::numeric_limits<int>::max()))
+        if (count > static_cast<size_t>(std::numeric_limits<int>::max() / adj::kLanes))
             fail(PBF_ERR_LENGTH, "Particle count exceeds CUDA kernel index range");
         if (maxnb <= 0) fail(PBF_ERR_INVALID_ARGUMENT, "maxNeighbors must be greater than zero");
         if (ckpt_every <= 0) fail(PBF_ERR_INVALID_ARGUMENT, "checkpoint interval must be positive");
@@ -492,6 +470,7 @@ struct pbf_adjoint {
         const std::array<int, 3> d = grid_dims_checked(lo, hi, p.smoothingRadius);
         cuda_check(cudaSetDevice(device));
         if (!stream) cuda_check(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+        clear_graphs();
         n = count;
         max_nb = maxnb;
         every = ckpt_every;
@@ -538,37 +517,34 @@ struct pbf_adjoint {
         c.col.cmaxz = hi.z;
 
         const size_t f4b = n * sizeof(float4), u4b = n * sizeof(uint32_t);
+        const size_t E = static_cast<size_t>(every), I = static_cast<size_t>(iters);
         keys.allocate(u4b);
         skeys.allocate(u4b);
-        sidx.allocate(u4b);
         akeys.allocate(u4b);
         aidx.allocate(u4b);
-        org.allocate(u4b);
+        orgs.allocate(2 * u4b);
         first.allocate((cells + 1) * sizeof(int));
-        xsorted.allocate(f4b);
         soa.allocate(3 * soa_stride() * sizeof(float));
-        nbr_s.allocate(stride * size_t(max_nb) * sizeof(uint32_t));
-        cnt_s.allocate(u4b);
         scratch.allocate(sort_scratch_bytes(static_cast<int>(n)));
         status.allocate(sizeof(unsigned));
-        tape4.allocate(static_cast<size_t>(every) * f4_slots() * f4b);
-        tapel.allocate(static_cast<size_t>(every) * iters * n * sizeof(float));
-        tapen.allocate(static_cast<size_t>(every) * (iters + 1) * stride * max_nb *
-                       sizeof(uint32_t));
-        tapec.allocate(static_cast<size_t>(every) * (iters + 1) * u4b);
-        for (DeviceBuffer* b : {&xa, &va, &xb, &vb, &gx, &gv, &gxs, &gv1, &gv3, &gq0, &gq1,
-                                &gpart, &aux})
+        for (DeviceBuffer* b : {&xs0, &vin, &pn}) b->allocate(f4b);
+        tf4.allocate(E * f4_per_step() * f4b);
+        tu32.allocate(E * u32_per_step() * u4b);
+        tlam.allocate(E * I * n * sizeof(float));
+        tmv.allocate(E * I * n);
+        tnb.allocate(E * (I + 1) * stride * max_nb * sizeof(uint32_t));
+        tcn.allocate(E * (I + 1) * u4b);
+        states.allocate((E + 1) * 2 * f4b);
+        for (DeviceBuffer* b : {&gx, &gv, &gxs, &gv1, &gv3, &gq0, &gq1, &gpart, &aux})
             b->allocate(f4b);
-        // Lists and counts start empty, so no stale index is ever read.
-        cuda_check(cudaMemsetAsync(tapen.get(), 0, tapen.bytes(), stream));
-        cuda_check(cudaMemsetAsync(tapec.get(), 0, tapec.bytes(), stream));
-        cuda_check(cudaMemsetAsync(nbr_s.get(), 0, nbr_s.bytes(), stream));
-        cuda_check(cudaMemsetAsync(cnt_s.get(), 0, cnt_s.bytes(), stream));
-        cuda_check(cudaMemsetAsync(sidx.get(), 0, sidx.bytes(), stream));
-        cuda_check(cudaStreamSynchronize(stream));
         aa.allocate(n * sizeof(float));
         acc_r.allocate(n * sizeof(double));
         acc_c.allocate(n * sizeof(double));
+        // Index data starts zeroed, so no index read after a failed step is
+        // ever out of range.
+        for (DeviceBuffer* b : {&tnb, &tcn, &tu32, &tmv, &orgs, &first, &keys})
+            cuda_check(cudaMemsetAsync(b->get(), 0, b->bytes(), stream));
+        cuda_check(cudaStreamSynchronize(stream));
         ckpt = DeviceBuffer();
         steps_done = 0;
     }
@@ -585,56 +561,109 @@ struct pbf_adjoint {
         c.gs = prm.particleMass / rest_density;
         c.gs2 = c.gs * c.gs;
         c.xsph_c = xsph;
+        clear_graphs();  // the graphs hold the old constants
         ckpt = DeviceBuffer();
         steps_done = 0;
     }
 
-    // Neighbour lists of p (particle-id order) into (nbr, cnt).
-    void build_lists(const float4* p, uint32_t* nbr, int* cnt) {
+    // Sort of the current keys into permutation rel, gather of src (the
+    // previous order) into dst, composed permutation into org_out.
+    void rebuild(const float4* src, float4* dst, uint32_t* rel, const uint32_t* org_in,
+                 uint32_t* org_out) {
         const int N = static_cast<int>(n);
         unsigned* sp = status.as<unsigned>();
-        launch_grid_keys(p, keys.as<uint32_t>(), N, c.g, stream);
-        launch_sort(plan, keys.as<uint32_t>(), skeys.as<uint32_t>(), sidx.as<uint32_t>(),
-                    akeys.as<uint32_t>(), aidx.as<uint32_t>(), scratch.get(), sp, stream);
         float* s0 = soa.as<float>();
-        launch_gather_first(sidx.as<uint32_t>(), p, xsorted.as<float4>(), nullptr,
-                            org.as<uint32_t>(), s0, s0 + soa_stride(), s0 + 2 * soa_stride(), N,
-                            skeys.as<uint32_t>(), cells, first.as<int>(), sp, stream);
-        launch_search(xsorted.as<float4>(), s0, s0 + soa_stride(), s0 + 2 * soa_stride(),
-                      first.as<int>(), c, N, nbr_s.as<uint32_t>(), cnt_s.as<int>(), nullptr, sp,
-                      false, stream);
-        adj::k_map_lists<<<adj::grid(N), adj::kB, 0, stream>>>(sidx.as<uint32_t>(),
-                                                               nbr_s.as<uint32_t>(),
-                                                               cnt_s.as<int>(), N, stride, max_nb,
-                                                               nbr, cnt);
+        launch_sort(plan, keys.as<uint32_t>(), skeys.as<uint32_t>(), rel, akeys.as<uint32_t>(),
+                    aidx.as<uint32_t>(), scratch.get(), sp, stream);
+        launch_gather_first(rel, src, dst, org_in, org_out, s0, s0 + soa_stride(),
+                            s0 + 2 * soa_stride(), N, skeys.as<uint32_t>(), cells, first.as<int>(),
+                            sp, stream);
     }
 
-    // One step from (x, v) to (x_out, v_out).  With a tape slot t >= 0 every
-    // intermediate goes to the tape; otherwise slot 0 of the tape is scratch.
-    void step(const float4* x, const float4* v, float4* x_out, float4* v_out, int t) {
+    // One step of the solver from (x, v) in particle-id order into tape slot
+    // t, leaving (x_out, v_out) in particle-id order.
+    void step(int t, const float4* x, const float4* v, float4* x_out, float4* v_out) {
         const int N = static_cast<int>(n);
-        const int s = t < 0 ? 0 : t;
         const int I = iters;
-        float4* v1 = T(s, 1);
-        cuda_check(cudaMemcpyAsync(T(s, 0), x, n * sizeof(float4), cudaMemcpyDeviceToDevice,
-                                   stream));
-        adj::k_integrate<<<adj::grid(N), adj::kB, 0, stream>>>(x, v, c, N, v1, T(s, 2));
+        unsigned* sp = status.as<unsigned>();
+        float* s0 = soa.as<float>();
+        uint32_t* oa = orgs.as<uint32_t>();
+        uint32_t* ob = oa + n;
+        launch_predict(x, v, xs0.as<float4>(), vin.as<float4>(), keys.as<uint32_t>(), N, c, sp,
+                       stream);
+        const float4* src = xs0.as<float4>();
+        const uint32_t* org_in = nullptr;
         for (int k = 0; k < I; ++k) {
-            build_lists(T(s, 2 + k), NB(s, k), CN(s, k));
-            adj::k_lambda<<<adj::grid(N), adj::kB, 0, stream>>>(T(s, 2 + k), NB(s, k), CN(s, k),
-                                                                c, N, L(s, k));
-            adj::k_delta<<<adj::grid(N), adj::kB, 0, stream>>>(T(s, 2 + k), L(s, k), NB(s, k),
-                                                               CN(s, k), c, N, T(s, 3 + I + k),
-                                                               T(s, 3 + k));
+            uint32_t* org_out = (k & 1) ? ob : oa;
+            rebuild(src, P(t, k), REL(t, k), org_in, org_out);
+            launch_search(P(t, k), s0, s0 + soa_stride(), s0 + 2 * soa_stride(), first.as<int>(), c,
+                          N, NB(t, k), CN(t, k), LAM(t, k), sp, true, stream);
+            launch_delta_apply(P(t, k), NB(t, k), CN(t, k), LAM(t, k), c, N, pn.as<float4>(),
+                               keys.as<uint32_t>(), sp, stream, MV(t, k));
+            src = pn.as<float4>();
+            org_in = org_out;
         }
-        float4* pI = T(s, 2 + I);
-        build_lists(pI, NB(s, I), CN(s, I));
-        adj::k_velocity<<<adj::grid(N), adj::kB, 0, stream>>>(pI, x, v1, c, N, T(s, 3 + 2 * I));
-        adj::k_xsph<<<adj::grid(N), adj::kB, 0, stream>>>(pI, T(s, 3 + 2 * I), NB(s, I),
-                                                          CN(s, I), c, N, T(s, 4 + 2 * I));
-        adj::k_respond<<<adj::grid(N), adj::kB, 0, stream>>>(pI, v1, T(s, 4 + 2 * I), c, N, v_out,
-                                                             x_out);
+        float4* pF = P(t, I);
+        rebuild(src, pF, REL(t, I), org_in, ORG(t));
+        launch_finalize(ORG(t), x, vin.as<float4>(), v, nullptr, pF, N, c, V2(t), VINF(t),
+                        nullptr, sp, stream);
+        launch_search_xsph(pF, s0, s0 + soa_stride(), s0 + 2 * soa_stride(), first.as<int>(), c, N,
+                           NB(t, I), CN(t, I), V2(t), V3(t), VINF(t), false, sp, stream);
+        adj::k_respond_out<<<adj::grid(N), adj::kB, 0, stream>>>(pF, VINF(t), V3(t), ORG(t), c, N,
+                                                                 x_out, v_out);
         cuda_check(cudaGetLastError());
+    }
+
+    // Adjoint of tape slot t: (gx, gv) of the step's output -> of its input,
+    // both in particle-id order.
+    void step_adjoint(int t) {
+        const int N = static_cast<int>(n);
+        const int I = iters;
+        float4* pF = P(t, I);
+        adj::k_respond_adj<<<adj::grid(N), adj::kB, 0, stream>>>(
+            pF, VINF(t), V3(t), gv.as<float4>(), ORG(t), c, N, gv3.as<float4>(),
+            gv1.as<float4>());
+        float4* gqa = gq0.as<float4>();
+        float4* gqb = gq1.as<float4>();
+        adj::k_xsph_adj<<<adj::grid_lanes(N), adj::kB, 0, stream>>>(
+            pF, V2(t), gv3.as<float4>(), NB(t, I), CN(t, I), gx.as<float4>(), ORG(t), REL(t, I),
+            MV(t, I - 1), c, N, gxs.as<float4>(), gqa, acc_c.as<double>());
+        for (int k = I - 1; k >= 0; --k) {
+            adj::k_iter_adj_a<<<adj::grid_lanes(N), adj::kB, 0, stream>>>(
+                P(t, k), LAM(t, k), gqa, NB(t, k), CN(t, k), c, N, gpart.as<float4>(),
+                aux.as<float4>(), aa.as<float>(), acc_r.as<double>());
+            adj::k_iter_adj_b<<<adj::grid_lanes(N), adj::kB, 0, stream>>>(
+                P(t, k), aux.as<float4>(), aa.as<float>(), NB(t, k), CN(t, k),
+                gpart.as<float4>(), REL(t, k), k > 0 ? MV(t, k - 1) : nullptr, gxs.as<float4>(),
+                gv1.as<float4>(), c, N, gqb, gx.as<float4>(), gv.as<float4>());
+            std::swap(gqa, gqb);
+        }
+        cuda_check(cudaGetLastError());
+    }
+
+    // Runs `enqueue` as a graph cached under key (captured on first use).
+    template <class F>
+    void run_graph(std::tuple<int, int, int> key, F&& enqueue) {
+        auto it = graphs.find(key);
+        if (it == graphs.end()) {
+            cuda_check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+            try {
+                enqueue();
+            } catch (...) {
+                cudaGraph_t g = nullptr;
+                cudaStreamEndCapture(stream, &g);
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
+            cudaGraph_t g = nullptr;
+            cuda_check(cudaStreamEndCapture(stream, &g));
+            cudaGraphExec_t ex = nullptr;
+            const cudaError_t e = cudaGraphInstantiate(&ex, g, 0);
+            cudaGraphDestroy(g);
+            cuda_check(e);
+            it = graphs.emplace(key, ex).first;
+        }
+        cuda_check(cudaGraphLaunch(it->second, stream));
     }
 
     void check_status() {
@@ -654,51 +683,29 @@ struct pbf_adjoint {
         const size_t f4b = n * sizeof(float4);
         const int nck = steps / every + 1;
         ckpt = DeviceBuffer(static_cast<size_t>(nck) * 2 * f4b);
+        steps_done = 0;
         cuda_check(cudaMemsetAsync(status.get(), 0, sizeof(unsigned), stream));
-        cuda_check(cudaMemcpyAsync(xa.get(), x0, f4b, cudaMemcpyDefault, stream));
-        cuda_check(cudaMemcpyAsync(va.get(), v0, f4b, cudaMemcpyDefault, stream));
-        float4 *x = xa.as<float4>(), *v = va.as<float4>();
-        float4 *xn = xb.as<float4>(), *vn = vb.as<float4>();
-        for (int t = 0; t < steps; ++t) {
-            if (t % every == 0) {
-                float4* ck = ckpt.as<float4>() + static_cast<size_t>(t / every) * 2 * n;
-                cuda_check(cudaMemcpyAsync(ck, x, f4b, cudaMemcpyDeviceToDevice, stream));
-                cuda_check(cudaMemcpyAsync(ck + n, v, f4b, cudaMemcpyDeviceToDevice, stream));
-            }
-            step(x, v, xn, vn, -1);
-            std::swap(x, xn);
-            std::swap(v, vn);
+        cuda_check(cudaMemcpyAsync(SX(0), x0, f4b, cudaMemcpyDefault, stream));
+        cuda_check(cudaMemcpyAsync(SV(0), v0, f4b, cudaMemcpyDefault, stream));
+        // The state after t steps is in slot t % 2.
+        for (int t0 = 0; t0 < steps; t0 += every) {
+            const int len = std::min(every, steps - t0);
+            const int par = t0 & 1;
+            float4* ck = ckpt.as<float4>() + static_cast<size_t>(t0 / every) * 2 * n;
+            cuda_check(cudaMemcpyAsync(ck, SX(par), f4b, cudaMemcpyDeviceToDevice, stream));
+            cuda_check(cudaMemcpyAsync(ck + n, SV(par), f4b, cudaMemcpyDeviceToDevice, stream));
+            run_graph(std::make_tuple(0, len, par), [&]() {
+                for (int t = 0; t < len; ++t) {
+                    const int a = (par + t) & 1;
+                    step(0, SX(a), SV(a), SX(1 - a), SV(1 - a));
+                }
+            });
         }
-        cuda_check(cudaMemcpyAsync(x_out, x, f4b, cudaMemcpyDefault, stream));
-        cuda_check(cudaMemcpyAsync(v_out, v, f4b, cudaMemcpyDefault, stream));
+        const int fin = steps & 1;
+        cuda_check(cudaMemcpyAsync(x_out, SX(fin), f4b, cudaMemcpyDefault, stream));
+        cuda_check(cudaMemcpyAsync(v_out, SV(fin), f4b, cudaMemcpyDefault, stream));
         check_status();
         steps_done = steps;
-    }
-
-    // Adjoint of the tape slot t: (gx, gv) of the step's output -> of its input.
-    void step_adjoint(int t) {
-        const int N = static_cast<int>(n);
-        const int I = iters;
-        float4* pI = T(t, 2 + I);
-        adj::k_respond_adj<<<adj::grid(N), adj::kB, 0, stream>>>(
-            pI, T(t, 1), T(t, 4 + 2 * I), gv.as<float4>(), c, N, gv3.as<float4>(),
-            gv1.as<float4>());
-        float4* gqa = gq0.as<float4>();
-        float4* gqb = gq1.as<float4>();
-        adj::k_xsph_adj<<<adj::grid(N), adj::kB, 0, stream>>>(
-            pI, T(t, 3 + 2 * I), gv3.as<float4>(), NB(t, I), CN(t, I), gx.as<float4>(),
-            T(t, 3 + I + (I - 1)), c, N, gxs.as<float4>(), gqa, acc_c.as<double>());
-        for (int k = I - 1; k >= 0; --k) {
-            adj::k_iter_adj_a<<<adj::grid(N), adj::kB, 0, stream>>>(
-                T(t, 2 + k), L(t, k), gqa, NB(t, k), CN(t, k), c, N, gpart.as<float4>(),
-                aux.as<float4>(), aa.as<float>(), acc_r.as<double>());
-            adj::k_iter_adj_b<<<adj::grid(N), adj::kB, 0, stream>>>(
-                T(t, 2 + k), aux.as<float4>(), aa.as<float>(), NB(t, k), CN(t, k),
-                gpart.as<float4>(), k > 0 ? T(t, 3 + I + (k - 1)) : nullptr, gxs.as<float4>(),
-                gv1.as<float4>(), c, N, gqb, gx.as<float4>(), gv.as<float4>());
-            std::swap(gqa, gqb);
-        }
-        cuda_check(cudaGetLastError());
     }
 
     void backward(const pbf_float4* gx_out, const pbf_float4* gv_out, pbf_float4* gx0,
@@ -718,16 +725,14 @@ struct pbf_adjoint {
             const int t0 = sg * every;
             const int len = std::min(every, steps_done - t0);
             const float4* ck = ckpt.as<float4>() + static_cast<size_t>(sg) * 2 * n;
-            cuda_check(cudaMemcpyAsync(xa.get(), ck, f4b, cudaMemcpyDeviceToDevice, stream));
-            cuda_check(cudaMemcpyAsync(va.get(), ck + n, f4b, cudaMemcpyDeviceToDevice, stream));
-            float4 *x = xa.as<float4>(), *v = va.as<float4>();
-            float4 *xn = xb.as<float4>(), *vn = vb.as<float4>();
-            for (int t = 0; t < len; ++t) {
-                step(x, v, xn, vn, t);
-                std::swap(x, xn);
-                std::swap(v, vn);
-            }
-            for (int t = len - 1; t >= 0; --t) step_adjoint(t);
+            cuda_check(cudaMemcpyAsync(SX(0), ck, f4b, cudaMemcpyDeviceToDevice, stream));
+            cuda_check(cudaMemcpyAsync(SV(0), ck + n, f4b, cudaMemcpyDeviceToDevice, stream));
+            run_graph(std::make_tuple(1, len, 0), [&]() {
+                for (int t = 0; t < len; ++t) step(t, SX(t), SV(t), SX(t + 1), SV(t + 1));
+            });
+            run_graph(std::make_tuple(2, len, 0), [&]() {
+                for (int t = len - 1; t >= 0; --t) step_adjoint(t);
+            });
         }
         cuda_check(cudaMemcpyAsync(gx0, gx.get(), f4b, cudaMemcpyDefault, stream));
         cuda_check(cudaMemcpyAsync(gv0, gv.get(), f4b, cudaMemcpyDefault, stream));

@@ -508,12 +508,13 @@ __device__ __forceinline__ void delta_sum(const StepConst& c, const float4* __re
 
 // delta p + applyDeltaPosition + CollisionSystem::solve + next cell keys.
 // N: artificial-pressure exponent fixed at compile time (0 = read at run time).
+// moved (optional): bit a set where the projection changed component a.
 template <int N, bool B>
 __global__ void __launch_bounds__(kMaxTunedBlock)
 k_delta_apply(const float4* __restrict__ xs, const uint32_t* __restrict__ nbr,
               const int* __restrict__ cnt, const float* __restrict__ lam, StepConst c, int n,
               float4* __restrict__ xs_out, uint32_t* __restrict__ keys_out,
-              unsigned* __restrict__ status) {
+              uint8_t* __restrict__ moved, unsigned* __restrict__ status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || fatal(status)) return;
     const float4 pi = xs[i];
@@ -526,8 +527,11 @@ k_delta_apply(const float4* __restrict__ xs, const uint32_t* __restrict__ nbr,
         delta_sum<N>(c, xs, nbr, lam, i, count, pi, gs, dpx, dpy, dpz);
     }
     float px = fadd(pi.x, dpx), py = fadd(pi.y, dpy), pz = fadd(pi.z, dpz);
+    const float ux = px, uy = py, uz = pz;
     if (!project_all(colliders_of<B>(c, i), c.particle_radius, px, py, pz))
         atomicOr(status, kStatusNotConverged);
+    if (moved)
+        moved[i] = static_cast<uint8_t>((px != ux) | ((py != uy) << 1) | ((pz != uz) << 2));
     const float4 q = make_float4(px, py, pz, pi.w);
     xs_out[i] = q;
     if (keys_out) {
@@ -559,7 +563,7 @@ k_finalize(const uint32_t* __restrict__ org, const float4* __restrict__ x_old,
     vv.w = v_old[o].w;
     v_new[i] = vv;
     vin_new[i] = vin_old[o];
-    id_new[i] = id_old[o];
+    if (id_new) id_new[i] = id_old[o];
 }
 
 // applyXsphViscosity (pbf_solver_kernels.cu:213-266).
@@ -942,11 +946,12 @@ void launch_search_xsph(const float4* xs, const float* sx, const float* sy, cons
 template <bool B>
 void launch_delta_apply_b(const float4* xs, const uint32_t* nbr, const int* cnt, const float* lam,
                           const StepConst& c, int n, float4* xs_out, uint32_t* keys_out,
-                          unsigned* status, cudaStream_t st) {
+                          uint8_t* moved, unsigned* status, cudaStream_t st) {
     const int bs = tuned_block(c, kTunedDelta);
     const unsigned g = blocks_for(n, bs);
 #define PBF_DELTA_CASE(N)                                                                        \
-    launch_k(k_delta_apply<N, B>, g, bs, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out, status)
+    launch_k(k_delta_apply<N, B>, g, bs, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out, moved,   \
+             status)
     switch (c.sc.k != 0.0f ? c.sc.n : 0) {
         case 1: PBF_DELTA_CASE(1); break;
         case 2: PBF_DELTA_CASE(2); break;
@@ -958,11 +963,11 @@ void launch_delta_apply_b(const float4* xs, const uint32_t* nbr, const int* cnt,
 }
 void launch_delta_apply(const float4* xs, const uint32_t* nbr, const int* cnt, const float* lam,
                         const StepConst& c, int n, float4* xs_out, uint32_t* keys_out,
-                        unsigned* status, cudaStream_t st) {
+                        unsigned* status, cudaStream_t st, uint8_t* moved) {
     if (c.scenes)
-        launch_delta_apply_b<true>(xs, nbr, cnt, lam, c, n, xs_out, keys_out, status, st);
+        launch_delta_apply_b<true>(xs, nbr, cnt, lam, c, n, xs_out, keys_out, moved, status, st);
     else
-        launch_delta_apply_b<false>(xs, nbr, cnt, lam, c, n, xs_out, keys_out, status, st);
+        launch_delta_apply_b<false>(xs, nbr, cnt, lam, c, n, xs_out, keys_out, moved, status, st);
 }
 void launch_finalize(const uint32_t* org, const float4* x_old, const float4* vin_old,
                      const float4* v_old, const uint32_t* id_old, const float4* xs, int n,

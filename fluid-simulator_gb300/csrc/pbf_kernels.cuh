@@ -93,9 +93,12 @@ void launch_search_xsph(const float4* xs, const float* sx, const float* sy, cons
                         const int* first, const StepConst& c, int n, uint32_t* nbr, int* cnt,
                         const float4* v, float4* v_out, const float4* vin, bool resolve,
                         unsigned* status, cudaStream_t st);
+// moved (optional): per slot, bit a set where the collision projection
+// changed component a of the position.
 void launch_delta_apply(const float4* xs, const uint32_t* nbr, const int* cnt, const float* lam,
                         const StepConst& c, int n, float4* xs_out, uint32_t* keys_out,
-                        unsigned* status, cudaStream_t st);
+                        unsigned* status, cudaStream_t st, uint8_t* moved = nullptr);
+// id_new may be null (ids not carried).
 void launch_finalize(const uint32_t* org, const float4* x_old, const float4* vin_old,
                      const float4* v_old, const uint32_t* id_old, const float4* xs, int n,
                      const StepConst& c, float4* v_new, float4* vin_new, uint32_t* id_new,
