@@ -279,6 +279,64 @@ def reference_cuda(scene, steps: int, warmup: int, max_neighbors: int = 256):
                       "step()"}
 
 
+def reference_scene(pkg, scenes, frames: int = 60, reps: int = 5, warmup: int = 10):
+    """The reference's own benchmark (benchmark/pbf_benchmark.cu:158-212):
+    262,144 particles, 2 substeps x 4 iterations, box + sphere; `warmup`
+    frames, then `reps` runs of `frames` frames, each from the initial state;
+    the run with the median average is reported as particle-frames/s and
+    particle-substeps/s.  The reference's kernels run the same scene on the
+    same GPU the same way."""
+    from oracle import oracle as O
+    from oracle import build_ref
+    pos, vel, mn, mx, prm, col = scenes.reference_benchmark()
+    n = len(pos)
+    sub = prm.substeps
+
+    def summary(run_ms):
+        med = sorted(run_ms)[len(run_ms) // 2]
+        return {"ms_per_frame": med / frames, "runs_ms": run_ms,
+                "particle_frames_per_s": n * frames / (med / 1000.0),
+                "particle_substeps_per_s": n * frames * sub / (med / 1000.0)}
+
+    s = pkg.PBFSolver()
+    s.initialize(n, mn, mx, prm)
+    s.set_spheres(col["spheres"])
+    s.set_boxes(col["boxes"])
+    s.set_particles(pos, vel)
+    s.run(warmup)
+    ours = []
+    for _ in range(reps):
+        s.set_particles(pos, vel)
+        ours.append(s.time_frames(frames))
+    s.close()
+    out = {"particles": n, "substeps": sub, "iterations": prm.solverIterations,
+           "frames": frames, "repetitions": reps, "warmup_frames": warmup,
+           "ours": summary(ours)}
+    if not build_ref.available():
+        out["reference_cuda"] = {"unavailable": "reference kernels not built"}
+        return out
+    r = O.RefCudaSolver()
+    r.initialize(n, mn, mx, prm.as_dict())
+    sp = [(*c, rr) for c, rr in col["spheres"]]
+    bx = [(*c, *e) for c, e in col["boxes"]]
+    r.set_colliders(np.asarray(sp, np.float32).reshape(-1, 4),
+                    np.asarray(bx, np.float32).reshape(-1, 6), np.zeros((0, 6), np.float32))
+    r.set_particles(pos, vel)
+    st = r.run(warmup)
+    ref = []
+    for _ in range(reps if st == 0 else 0):
+        r.set_particles(pos, vel)
+        ref.append(r.time_steps(frames))
+    r.close()
+    if st != 0:
+        out["reference_cuda"] = {"unavailable": "reference step failed with status %d" % st}
+        return out
+    out["reference_cuda"] = summary(ref)
+    out["speedup"] = (out["ours"]["particle_frames_per_s"]
+                      / out["reference_cuda"]["particle_frames_per_s"])
+    return out
+
+
 def batched(pkg, scenes, steps: int, warmup: int, per_scene_steps: int):
     """256 independent scenes (particle counts log-uniform in [2,048, 65,536])
     stepped by one batched solver -- one launch per stage for all scenes --
@@ -535,6 +593,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default 256-thread blocks")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-reference-scene", action="store_true",
+                    help="skip the reference's own 262,144-particle benchmark scene")
     ap.add_argument("--adjoint-steps", type=int, default=60)
     ap.add_argument("--adjoint-directions", type=int, default=8)
     ap.add_argument("--batched-steps", type=int, default=120)
@@ -673,6 +733,8 @@ def main():
                                                     args.max_neighbors)
             if "value" in line["reference_cuda"]:
                 line["speedup_vs_reference_cuda"] = value / line["reference_cuda"]["value"]
+        if world == 1 and not args.no_reference_scene:
+            line["reference_scene"] = reference_scene(pkg, scenes)
         if world == 1 and not args.no_batched:
             line["batched"] = batched(pkg, scenes, args.batched_steps, args.warmup,
                                       args.per_scene_steps)

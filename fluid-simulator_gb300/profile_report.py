@@ -72,6 +72,28 @@ def child(scene: str, warmup: int, frames: int):
     print("kernels_per_frame %d" % s.kernels_per_frame(), flush=True)
 
 
+def child_adjoint(steps: int):
+    """The profiled adjoint workload: 65,536 particles (64x64x16 dam-break
+    lattice, vorticity off), a `steps`-step forward with one checkpoint
+    segment, then the backward (recompute into the tape, adjoint passes)."""
+    import numpy as np
+    pkg = load_pkg()
+    scenes = importlib.import_module("fluid_simulator_gb300.scenes")
+    nx, ny, nz = 64, 64, 16
+    S = scenes.SPACING
+    pos, vel, mn, mx, prm, _ = scenes.dam_break(nx, ny, nz, (2 * nx * S, 1.5 * ny * S, 2 * nz * S))
+    prm.vorticityStrength = 0.0
+    n = len(pos)
+    a = pkg.PBFAdjoint()
+    a.initialize(n, mn, mx, prm, max_neighbors=128, checkpoint_every=steps)
+    x, _ = a.forward(pos, vel, steps)
+    gx = np.zeros((n, 4), np.float32)
+    gx[:, :3] = (2.0 / n) * (x[:, :3] - pos[:, :3] - np.array([0.3, 0.0, 0.0], np.float32))
+    a.backward(gx, np.zeros_like(gx))
+    a.close()
+    print("kernels_per_frame 0", flush=True)
+
+
 def run(cmd, **kw):
     r = subprocess.run(cmd, capture_output=True, text=True, **kw)
     if r.returncode != 0:
@@ -112,14 +134,24 @@ def main():
     ap.add_argument("--top", type=int, default=4)
     ap.add_argument("--ncu", default="ncu")
     ap.add_argument("--out", default=None)
+    ap.add_argument("--adjoint", action="store_true",
+                    help="profile the adjoint (forward + backward of --adjoint-steps steps at "
+                         "65,536 particles) instead of a solver frame")
+    ap.add_argument("--adjoint-steps", type=int, default=10)
     ap.add_argument("--child", action="store_true")
     args = ap.parse_args()
     if args.child:
-        child(args.scene, args.warmup, 1)
+        if args.adjoint:
+            child_adjoint(args.adjoint_steps)
+        else:
+            child(args.scene, args.warmup, 1)
         return 0
 
     me = [sys.executable, os.path.abspath(__file__), "--child", "--scene", args.scene,
           "--warmup", str(args.warmup)]
+    if args.adjoint:
+        me = [sys.executable, os.path.abspath(__file__), "--child", "--adjoint",
+              "--adjoint-steps", str(args.adjoint_steps)]
     root = os.path.dirname(HERE)
 
     def shown(cmd):
@@ -137,12 +169,14 @@ def main():
 
     out = run(me)  # plain run first: it must succeed before ncu sees it
     kpf = int(out.split("kernels_per_frame")[1].split()[0])
-    before = 2 + args.warmup * kpf  # set_particles launches two kernels
+    # Solver: skip set_particles (two kernels) and the warm-up frames, list
+    # one frame.  Adjoint: list every launch of the forward and backward.
+    before = 0 if args.adjoint else 2 + args.warmup * kpf
     tmp = tempfile.mkdtemp(prefix="pbf_prof_")
     lst = os.path.join(tmp, "launches.csv")
+    window = [] if args.adjoint else ["--launch-count", str(kpf)]
     cmd1 = [args.ncu, "--metrics", "gpu__time_duration.sum", "--clock-control", "none",
-            "--launch-skip", str(before), "--launch-count", str(kpf), "--csv", "--log-file",
-            lst] + me
+            "--launch-skip", str(before)] + window + ["--csv", "--log-file", lst] + me
     run(cmd1)
     agg = {}
     rows = [r for r in ncu_rows(lst) if r["Metric Name"] == "gpu__time_duration.sum"]
@@ -173,14 +207,22 @@ def main():
             vals[r["Metric Name"]] = value(r)
         detail[k] = vals
 
-    lines = ["# Kernel profile: %s, one frame after %d warm-up frames" % (args.scene,
-                                                                         args.warmup), "",
-             "Generated by:", "",
-             "    python fluid-simulator_gb300/profile_report.py --scene %s --warmup %d --top %d"
-             % (args.scene, args.warmup, args.top), "",
+    if args.adjoint:
+        title = ("# Kernel profile: adjoint, 65,536 particles, %d-step forward + backward"
+                 % args.adjoint_steps)
+        gen = ("    python fluid-simulator_gb300/profile_report.py --adjoint --adjoint-steps %d "
+               "--top %d" % (args.adjoint_steps, args.top))
+        unit = "launches"
+    else:
+        title = "# Kernel profile: %s, one frame after %d warm-up frames" % (args.scene,
+                                                                            args.warmup)
+        gen = ("    python fluid-simulator_gb300/profile_report.py --scene %s --warmup %d --top %d"
+               % (args.scene, args.warmup, args.top))
+        unit = "launches / frame"
+    lines = [title, "", "Generated by:", "", gen, "",
              "which runs (each after the same workload exited 0 without ncu):", ""]
     lines += ["    " + c for c in cmds]
-    lines += ["", "| kernel | launches / frame | device us | share |", "|---|---|---|---|"]
+    lines += ["", "| kernel | %s | device us | share |" % unit, "|---|---|---|---|"]
     for k, (cnt, sec, _) in order:
         lines.append("| %s | %d | %.1f | %.1f%% |" % (k, cnt, sec * 1e6, 100.0 * sec / total))
     lines += ["", "Top kernels, one launch each:", "",
