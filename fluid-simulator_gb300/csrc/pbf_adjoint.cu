@@ -35,9 +35,10 @@
 // result is deterministic.
 //
 // Checkpointing: the forward keeps (x, v) every K steps, in particle-id
-// order; the backward recomputes each K-step segment from its checkpoint into
-// the tape and runs the segment's adjoint in reverse.  Forward, recompute and
-// adjoint segments run as CUDA graphs.
+// order, and records its last segment into the tape; the backward recomputes
+// each earlier K-step segment from its checkpoint into the tape and runs the
+// segment's adjoint in reverse.  Forward, recompute and adjoint segments run
+// as CUDA graphs.
 #include "pbf_common.h"
 #include "pbf_kernels.cuh"
 
@@ -71,7 +72,7 @@ __device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a
 //   poly6 gradient grad W = -6 c_poly6 t^2 / h^2 r,  t = 1 - |r|^2 / h^2
 //   s_corr'        ds/d(d2) = 3 k n ratio^(3n-1) / (h^2 - dq^2)
 struct PairTerms {
-    float3 g;      // spiky gradient (the forward's rounding: spiky())
+    float3 g;      // spiky gradient
     float f, fpr;  // f and f'(rr) / rr
     float w;       // poly6
     float3 gw;     // poly6 gradient
@@ -81,30 +82,29 @@ struct PairTerms {
 __device__ __forceinline__ PairTerms pair_terms(const StepConst& c, float3 r) {
     PairTerms t;
     const float d2 = dist2(r.x, r.y, r.z);
-    spiky(c.k, r.x, r.y, r.z, d2, t.g.x, t.g.y, t.g.z);
+    t.g = t.gw = make_float3(0.0f, 0.0f, 0.0f);
+    t.f = t.fpr = t.w = t.s = t.sp = 0.0f;
+    if (!(d2 < c.k.h2)) return t;  // every term vanishes at |r| >= h
+    const float tp = 1.0f - d2 * c.k.inv_h2;
     t.w = poly6(c.k, d2);
-    t.s = scorr<0>(c.sc, d2);
-    t.f = 0.0f;
-    t.fpr = 0.0f;
-    t.sp = 0.0f;
-    t.gw = make_float3(0.0f, 0.0f, 0.0f);
-    if (d2 < c.k.h2) {
-        const float tp = 1.0f - d2 * c.k.inv_h2;
-        t.gw = (-6.0f * c.k.c_poly6 * tp * tp * c.k.inv_h2) * r;
-        if (d2 >= kSpikyMinD2) {
-            const float rr = sqrtf(d2);
-            const float u = 1.0f - rr * c.k.inv_h;
-            t.f = c.k.c_spiky * u * u / rr;
-            const float fp = -c.k.c_spiky * u / rr * (2.0f * c.k.inv_h + u / rr);
-            t.fpr = fp / rr;
-        }
-        if (c.sc.k != 0.0f && c.sc.n > 0 && c.sc.dq2 < c.sc.h2) {
-            // ratio^(3n - 1) = (ratio^3)^(n - 1) ratio^2.
-            const float ratio = (c.sc.h2 - d2) * c.sc.inv_den;
-            const float r2 = ratio * ratio;
-            t.sp = 3.0f * c.sc.k * static_cast<float>(c.sc.n) * ipow(r2 * ratio, c.sc.n - 1) *
-                   r2 * c.sc.inv_den;
-        }
+    t.gw = (-6.0f * c.k.c_poly6 * tp * tp * c.k.inv_h2) * r;
+    if (d2 >= kSpikyMinD2) {
+        // One reciprocal square root serves |r|, f, f' and the gradient.
+        const float ir = rsqrtf(d2);
+        const float rr = d2 * ir;
+        const float u = 1.0f - rr * c.k.inv_h;
+        t.f = c.k.c_spiky * u * u * ir;
+        t.g = t.f * r;
+        t.fpr = -c.k.c_spiky * u * ir * (2.0f * c.k.inv_h + u * ir) * ir;
+    }
+    if (c.sc.k != 0.0f && c.sc.n > 0 && c.sc.dq2 < c.sc.h2) {
+        // s = -k ratio^(3n), ds/d(d2) = 3 k n ratio^(3n - 1) / (h^2 - dq^2),
+        // with ratio^(3n - 1) = (ratio^3)^(n - 1) ratio^2.
+        const float ratio = (c.sc.h2 - d2) * c.sc.inv_den;
+        const float r2 = ratio * ratio;
+        const float pm1 = ipow(r2 * ratio, c.sc.n - 1);
+        t.s = c.sc.negk * pm1 * r2 * ratio;
+        t.sp = 3.0f * c.sc.k * static_cast<float>(c.sc.n) * pm1 * r2 * c.sc.inv_den;
     }
     return t;
 }
@@ -112,17 +112,20 @@ __device__ __forceinline__ float3 hess(const PairTerms& t, float3 r, float3 u) {
     return t.f * u + (t.fpr * dot3(r, u)) * r;
 }
 
-// The gather passes give each particle kLanes consecutive threads: lane l
-// takes list entries l, l + kLanes, ...; the partial sums are combined by a
-// fixed butterfly (deterministic), after which every lane holds the total.
+// The gather passes give each particle L consecutive threads (L = 2 or 4):
+// lane l takes list entries l, l + L, ...; the partial sums are combined by
+// a fixed butterfly (deterministic), after which every lane holds the
+// total.  More lanes, more warps to hide the gather latency.
 constexpr int kLanes = 4;
+template <int L>
 __device__ __forceinline__ float lane_sum(float v) {
 #pragma unroll
-    for (int m = 1; m < kLanes; m <<= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
+    for (int m = 1; m < L; m <<= 1) v += __shfl_xor_sync(0xffffffffu, v, m);
     return v;
 }
+template <int L>
 __device__ __forceinline__ float3 lane_sum(float3 v) {
-    return make_float3(lane_sum(v.x), lane_sum(v.y), lane_sum(v.z));
+    return make_float3(lane_sum<L>(v.x), lane_sum<L>(v.y), lane_sum<L>(v.z));
 }
 
 // ---- adjoint -----------------------------------------------------------------
@@ -210,6 +213,7 @@ __device__ __forceinline__ float4 unmoved(uint8_t m, float3 g) {
 //   dL/dc += gv3_i . sum_j (v2_j - v2_i) W_ij
 //   gq_{I-1} at slot rel[s] of the last iteration's order = gp_F where the
 //   projection left the component unchanged, 0 elsewhere.
+template <int L>
 __global__ void k_xsph_adj(const float4* __restrict__ pF, const float4* __restrict__ v2,
                            const float4* __restrict__ gv3, const uint32_t* __restrict__ nbr,
                            const int* __restrict__ cnt, const float4* __restrict__ gx_next,
@@ -218,13 +222,13 @@ __global__ void k_xsph_adj(const float4* __restrict__ pF, const float4* __restri
                            float4* __restrict__ gxs, float4* __restrict__ gq,
                            double* __restrict__ acc_c) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = tid / kLanes, lane = tid % kLanes;
+    const int i = tid / L, lane = tid % L;
     const bool live = i < n;
     const int ii = live ? i : 0;
     const float3 pi = f3(pF[ii]), vi = f3(v2[ii]), gi = f3(gv3[ii]);
     const int count = live ? min(cnt[i], c.max_nb) : 0;
     float3 sg = make_float3(0.0f, 0.0f, 0.0f), sv = sg, pos = sg;
-    for (int k = lane; k < count; k += kLanes) {
+    for (int k = lane; k < count; k += L) {
         const uint32_t j = __ldg(&nbr[static_cast<size_t>(k) * c.stride + i]);
         const float3 r = pi - f3(__ldg(&pF[j]));
         const PairTerms t = pair_terms(c, r);
@@ -234,9 +238,9 @@ __global__ void k_xsph_adj(const float4* __restrict__ pF, const float4* __restri
         sv = sv + t.w * dv;
         pos = pos + dot3(gi - gj, dv) * t.gw;
     }
-    sg = lane_sum(sg);
-    sv = lane_sum(sv);
-    pos = lane_sum(pos);
+    sg = lane_sum<L>(sg);
+    sv = lane_sum<L>(sv);
+    pos = lane_sum<L>(pos);
     if (!live || lane != 0) return;
     const float3 gv2 = gi + c.xsph_c * sg;
     acc_c[i] += static_cast<double>(dot3(gi, sv));
@@ -254,13 +258,14 @@ __global__ void k_xsph_adj(const float4* __restrict__ pF, const float4* __restri
 //   gC_i = -glam_i / D_i, gD_i = glam_i C_i / D_i^2, a_i = m gC_i / rho0,
 // with the rest-density partial gC_i (-rho_i / rho0^2) + g_gs_i (-m / rho0^2),
 // g_gs_i = gq_i . X_i + 2 gs gD_i (S2_i + |G_i|^2), X_i = delta p_i / gs.
+template <int L>
 __global__ void k_iter_adj_a(const float4* __restrict__ p, const float* __restrict__ lam,
                              const float4* __restrict__ gq, const uint32_t* __restrict__ nbr,
                              const int* __restrict__ cnt, StepConst c, int n,
                              float4* __restrict__ gpart, float4* __restrict__ aux,
                              float* __restrict__ aa, double* __restrict__ acc_rho0) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = tid / kLanes, lane = tid % kLanes;
+    const int i = tid / L, lane = tid % L;
     const bool live = i < n;
     const int ii = live ? i : 0;
     const float3 pi = f3(p[ii]), gqi = f3(gq[ii]);
@@ -268,7 +273,7 @@ __global__ void k_iter_adj_a(const float4* __restrict__ p, const float* __restri
     const int count = live ? min(cnt[i], c.max_nb) : 0;
     float wsum = 0.0f, s2 = 0.0f, glam = 0.0f;
     float3 G = make_float3(0.0f, 0.0f, 0.0f), X = G, dpos = G;
-    for (int k = lane; k < count; k += kLanes) {
+    for (int k = lane; k < count; k += L) {
         const uint32_t j = __ldg(&nbr[static_cast<size_t>(k) * c.stride + i]);
         const float3 r = pi - f3(__ldg(&p[j]));
         const PairTerms t = pair_terms(c, r);
@@ -282,12 +287,12 @@ __global__ void k_iter_adj_a(const float4* __restrict__ p, const float* __restri
         glam += ug;
         dpos = dpos + coef * hess(t, r, u) + (2.0f * t.sp * ug) * r;
     }
-    wsum = lane_sum(wsum) + c.k.c_poly6;
-    s2 = lane_sum(s2);
-    glam = lane_sum(glam);
-    G = lane_sum(G);
-    X = lane_sum(X);
-    dpos = lane_sum(dpos);
+    wsum = lane_sum<L>(wsum) + c.k.c_poly6;
+    s2 = lane_sum<L>(s2);
+    glam = lane_sum<L>(glam);
+    G = lane_sum<L>(G);
+    X = lane_sum<L>(X);
+    dpos = lane_sum<L>(dpos);
     if (!live || lane != 0) return;
     const float rho = c.mass * wsum;
     const float S = s2 + dot3(G, G);
@@ -312,6 +317,7 @@ __global__ void k_iter_adj_a(const float4* __restrict__ p, const float* __restri
 // order): either the projection of the previous iteration (gq_{k-1}) or,
 // after the first iteration, the integration adjoint (gx_t, gv_t in
 // particle-id order).
+template <int L>
 __global__ void k_iter_adj_b(const float4* __restrict__ p, const float4* __restrict__ aux,
                              const float* __restrict__ aa, const uint32_t* __restrict__ nbr,
                              const int* __restrict__ cnt, const float4* __restrict__ gpart,
@@ -321,7 +327,7 @@ __global__ void k_iter_adj_b(const float4* __restrict__ p, const float4* __restr
                              StepConst c, int n, float4* __restrict__ gq_prev,
                              float4* __restrict__ gx_t, float4* __restrict__ gv_t) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = tid / kLanes, lane = tid % kLanes;
+    const int i = tid / L, lane = tid % L;
     const bool live = i < n;
     const int ii = live ? i : 0;
     const float3 pi = f3(p[ii]);
@@ -330,7 +336,7 @@ __global__ void k_iter_adj_b(const float4* __restrict__ p, const float4* __restr
     const float gDi = ai4.w, ai = aa[ii];
     const int count = live ? min(cnt[i], c.max_nb) : 0;
     float3 acc = make_float3(0.0f, 0.0f, 0.0f);
-    for (int k = lane; k < count; k += kLanes) {
+    for (int k = lane; k < count; k += L) {
         const uint32_t j = __ldg(&nbr[static_cast<size_t>(k) * c.stride + i]);
         const float3 r = pi - f3(__ldg(&p[j]));
         const PairTerms t = pair_terms(c, r);
@@ -339,7 +345,7 @@ __global__ void k_iter_adj_b(const float4* __restrict__ p, const float4* __restr
         const float3 w = (gDi + gDj) * t.g + gDi * Gi - gDj * f3(aj4);
         acc = acc + (ai + __ldg(&aa[j])) * t.gw + (2.0f * c.gs2) * hess(t, r, w);
     }
-    acc = lane_sum(acc);
+    acc = lane_sum<L>(acc);
     if (!live || lane != 0) return;
     const float3 gp = f3(gpart[i]) + acc;
     const uint32_t r = rel[i];
@@ -373,10 +379,17 @@ __global__ void k_respond_out(const float4* __restrict__ pF, const float4* __res
 
 constexpr int kB = 256;
 inline unsigned grid(int n) { return static_cast<unsigned>((n + kB - 1) / kB); }
-// Grid of the gather passes (kLanes threads per particle).
-inline unsigned grid_lanes(int n) {
-    return static_cast<unsigned>((static_cast<size_t>(n) * kLanes + kB - 1) / kB);
+// Grid of the gather passes (L threads per particle).
+inline unsigned grid_lanes(int n, int L) {
+    return static_cast<unsigned>((static_cast<size_t>(n) * L + kB - 1) / kB);
 }
+// Lanes per particle of the gather passes: four while fewer than 2^17
+// particles leave the SMs short of warps, two above.  Backward time over
+// the solver's forward, 60 steps, lanes 1 / 2 / 4: 1.97 / 1.64 / 1.62 at
+// 65,536 particles, 2.04 / 1.89 / 1.95 at 262,144, 2.20 / 2.19 / 2.39 at
+// 1,048,576.
+constexpr int kLanesBelow = 1 << 17;
+inline int lanes_for(int n) { return n < kLanesBelow ? kLanes : 2; }
 
 }  // namespace adj
 }  // namespace pbf
@@ -406,6 +419,9 @@ struct pbf_adjoint {
     DeviceBuffer states;
     // Checkpoints (x, v) every `every` steps.
     DeviceBuffer ckpt;
+    // The tape holds the last segment of the latest forward (recorded by the
+    // forward itself, so the backward need not recompute it).
+    bool tape_last = false;
     // Adjoint work arrays.
     DeviceBuffer gx, gv, gxs, gv1, gv3, gq0, gq1, gpart, aux, aa, acc_r, acc_c;
     // Captured segments: (kind, length, parity) -> graph.
@@ -546,6 +562,7 @@ struct pbf_adjoint {
             cuda_check(cudaMemsetAsync(b->get(), 0, b->bytes(), stream));
         cuda_check(cudaStreamSynchronize(stream));
         ckpt = DeviceBuffer();
+        tape_last = false;
         steps_done = 0;
     }
 
@@ -563,6 +580,7 @@ struct pbf_adjoint {
         c.xsph_c = xsph;
         clear_graphs();  // the graphs hold the old constants
         ckpt = DeviceBuffer();
+        tape_last = false;
         steps_done = 0;
     }
 
@@ -617,22 +635,31 @@ struct pbf_adjoint {
     // Adjoint of tape slot t: (gx, gv) of the step's output -> of its input,
     // both in particle-id order.
     void step_adjoint(int t) {
+        if (adj::lanes_for(static_cast<int>(n)) == adj::kLanes)
+            step_adjoint_l<adj::kLanes>(t);
+        else
+            step_adjoint_l<2>(t);
+    }
+
+    template <int L>
+    void step_adjoint_l(int t) {
         const int N = static_cast<int>(n);
         const int I = iters;
+        const unsigned gl = adj::grid_lanes(N, L);
         float4* pF = P(t, I);
         adj::k_respond_adj<<<adj::grid(N), adj::kB, 0, stream>>>(
             pF, VINF(t), V3(t), gv.as<float4>(), ORG(t), c, N, gv3.as<float4>(),
             gv1.as<float4>());
         float4* gqa = gq0.as<float4>();
         float4* gqb = gq1.as<float4>();
-        adj::k_xsph_adj<<<adj::grid_lanes(N), adj::kB, 0, stream>>>(
+        adj::k_xsph_adj<L><<<gl, adj::kB, 0, stream>>>(
             pF, V2(t), gv3.as<float4>(), NB(t, I), CN(t, I), gx.as<float4>(), ORG(t), REL(t, I),
             MV(t, I - 1), c, N, gxs.as<float4>(), gqa, acc_c.as<double>());
         for (int k = I - 1; k >= 0; --k) {
-            adj::k_iter_adj_a<<<adj::grid_lanes(N), adj::kB, 0, stream>>>(
+            adj::k_iter_adj_a<L><<<gl, adj::kB, 0, stream>>>(
                 P(t, k), LAM(t, k), gqa, NB(t, k), CN(t, k), c, N, gpart.as<float4>(),
                 aux.as<float4>(), aa.as<float>(), acc_r.as<double>());
-            adj::k_iter_adj_b<<<adj::grid_lanes(N), adj::kB, 0, stream>>>(
+            adj::k_iter_adj_b<L><<<gl, adj::kB, 0, stream>>>(
                 P(t, k), aux.as<float4>(), aa.as<float>(), NB(t, k), CN(t, k),
                 gpart.as<float4>(), REL(t, k), k > 0 ? MV(t, k - 1) : nullptr, gxs.as<float4>(),
                 gv1.as<float4>(), c, N, gqb, gx.as<float4>(), gv.as<float4>());
@@ -684,28 +711,48 @@ struct pbf_adjoint {
         const int nck = steps / every + 1;
         ckpt = DeviceBuffer(static_cast<size_t>(nck) * 2 * f4b);
         steps_done = 0;
+        tape_last = false;
         cuda_check(cudaMemsetAsync(status.get(), 0, sizeof(unsigned), stream));
         cuda_check(cudaMemcpyAsync(SX(0), x0, f4b, cudaMemcpyDefault, stream));
         cuda_check(cudaMemcpyAsync(SV(0), v0, f4b, cudaMemcpyDefault, stream));
-        // The state after t steps is in slot t % 2.
+        // Before the last segment the state after t steps is in slot t % 2
+        // and the tape's slot 0 is scratch; the last segment runs as the
+        // backward's recompute would, into the tape.
+        int fin = 0;
         for (int t0 = 0; t0 < steps; t0 += every) {
             const int len = std::min(every, steps - t0);
             const int par = t0 & 1;
             float4* ck = ckpt.as<float4>() + static_cast<size_t>(t0 / every) * 2 * n;
             cuda_check(cudaMemcpyAsync(ck, SX(par), f4b, cudaMemcpyDeviceToDevice, stream));
             cuda_check(cudaMemcpyAsync(ck + n, SV(par), f4b, cudaMemcpyDeviceToDevice, stream));
-            run_graph(std::make_tuple(0, len, par), [&]() {
-                for (int t = 0; t < len; ++t) {
-                    const int a = (par + t) & 1;
-                    step(0, SX(a), SV(a), SX(1 - a), SV(1 - a));
+            if (t0 + len < steps) {
+                run_graph(std::make_tuple(0, len, par), [&]() {
+                    for (int t = 0; t < len; ++t) {
+                        const int a = (par + t) & 1;
+                        step(0, SX(a), SV(a), SX(1 - a), SV(1 - a));
+                    }
+                });
+                fin = (par + len) & 1;
+            } else {
+                if (par) {
+                    cuda_check(cudaMemcpyAsync(SX(0), ck, f4b, cudaMemcpyDeviceToDevice, stream));
+                    cuda_check(
+                        cudaMemcpyAsync(SV(0), ck + n, f4b, cudaMemcpyDeviceToDevice, stream));
                 }
-            });
+                run_graph(std::make_tuple(1, len, 0), [&]() { record(len); });
+                fin = len;
+                tape_last = true;
+            }
         }
-        const int fin = steps & 1;
         cuda_check(cudaMemcpyAsync(x_out, SX(fin), f4b, cudaMemcpyDefault, stream));
         cuda_check(cudaMemcpyAsync(v_out, SV(fin), f4b, cudaMemcpyDefault, stream));
         check_status();
         steps_done = steps;
+    }
+
+    // `len` steps from state slot 0 into tape slots 0..len-1 (states 1..len).
+    void record(int len) {
+        for (int t = 0; t < len; ++t) step(t, SX(t), SV(t), SX(t + 1), SV(t + 1));
     }
 
     void backward(const pbf_float4* gx_out, const pbf_float4* gv_out, pbf_float4* gx0,
@@ -724,12 +771,13 @@ struct pbf_adjoint {
         for (int sg = segs - 1; sg >= 0; --sg) {
             const int t0 = sg * every;
             const int len = std::min(every, steps_done - t0);
-            const float4* ck = ckpt.as<float4>() + static_cast<size_t>(sg) * 2 * n;
-            cuda_check(cudaMemcpyAsync(SX(0), ck, f4b, cudaMemcpyDeviceToDevice, stream));
-            cuda_check(cudaMemcpyAsync(SV(0), ck + n, f4b, cudaMemcpyDeviceToDevice, stream));
-            run_graph(std::make_tuple(1, len, 0), [&]() {
-                for (int t = 0; t < len; ++t) step(t, SX(t), SV(t), SX(t + 1), SV(t + 1));
-            });
+            if (!(sg == segs - 1 && tape_last)) {
+                const float4* ck = ckpt.as<float4>() + static_cast<size_t>(sg) * 2 * n;
+                cuda_check(cudaMemcpyAsync(SX(0), ck, f4b, cudaMemcpyDeviceToDevice, stream));
+                cuda_check(cudaMemcpyAsync(SV(0), ck + n, f4b, cudaMemcpyDeviceToDevice, stream));
+                run_graph(std::make_tuple(1, len, 0), [&]() { record(len); });
+            }
+            tape_last = false;  // the tape now holds this segment
             run_graph(std::make_tuple(2, len, 0), [&]() {
                 for (int t = len - 1; t >= 0; --t) step_adjoint(t);
             });

@@ -83,6 +83,22 @@ def test_forward_restarts_from_its_own_state(pbf, scenes):
     np.testing.assert_array_equal(v, v7)
 
 
+def test_backward_repeats_bit_for_bit(pbf, scenes):
+    # The first backward uses the last segment the forward recorded; the
+    # second recomputes it from its checkpoint.
+    pos, vel, mn, mx, prm, target = scene(scenes)
+    a = pbf.PBFAdjoint()
+    a.initialize(len(pos), mn, mx, prm, max_neighbors=128, checkpoint_every=3)
+    x, _ = a.forward(pos, vel, 7)
+    _, gx = loss_grad(x, target)
+    first = a.backward(gx, np.zeros_like(gx))
+    second = a.backward(gx, np.zeros_like(gx))
+    a.close()
+    np.testing.assert_array_equal(first[0], second[0])
+    np.testing.assert_array_equal(first[1], second[1])
+    assert first[2] == second[2] and first[3] == second[3]
+
+
 def test_adjoint_matches_fp64_forward_mode_and_finite_differences(pbf, scenes, orc):
     pos, vel, mn, mx, prm, target = scene(scenes)
     steps, every = 6, 4  # two segments, the second shorter
