@@ -139,11 +139,16 @@ void launch_integrate(const float4* x, float4* xs, float4* v, int n, const StepC
 // --- stable LSD radix sort of (key, index) pairs (pbf_sort.cu) ---------------
 struct SortPlan {
     int n = 0;
+    int tile = 0;  // keys per tile
     int tiles = 0;
     int passes = 0;
     int bits_per_pass = 0;
     int bins = 0;
 };
+// Smallest tile (keys) any plan uses, and the most digit bins of a pass:
+// the scratch of n keys holds (ceil(n / kSortMinTile) + 1) * kSortMaxBins words.
+constexpr int kSortMinTile = 1024;
+constexpr int kSortMaxBins = 256;
 SortPlan make_sort_plan(int n, uint64_t num_cells);
 // Scratch bytes for hist/totals of a plan with up to n keys.
 size_t sort_scratch_bytes(int max_n);

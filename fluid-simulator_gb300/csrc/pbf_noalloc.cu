@@ -26,8 +26,9 @@ constexpr size_t kKeysBytes = kStaticScratchParticles * sizeof(uint32_t);
 // Sort scratch (tile histograms + digit totals) for the capacity above,
 // rounded up to the array's alignment.
 constexpr size_t align256(size_t b) { return (b + 255) / 256 * 256; }
-constexpr size_t kSortBytes = align256(((kStaticScratchParticles + 4095) / 4096 + 1) * 256 * 4);
-constexpr size_t kScratchBytes = 3 * kKeysBytes + kSortBytes;  // about 3.1 MB
+constexpr size_t kSortBytes = align256(
+    ((kStaticScratchParticles + kSortMinTile - 1) / kSortMinTile + 1) * kSortMaxBins * 4);
+constexpr size_t kScratchBytes = 3 * kKeysBytes + kSortBytes;  // about 3.4 MB
 
 // Every GPU that loads the library holds this array until the process exits.
 static __device__ __align__(256) unsigned char g_static_scratch[kScratchBytes];
