@@ -599,6 +599,9 @@ def main():
     ap.add_argument("--adjoint-directions", type=int, default=8)
     ap.add_argument("--batched-steps", type=int, default=120)
     ap.add_argument("--per-scene-steps", type=int, default=20)
+    ap.add_argument("--list-capacity", type=int, default=None,
+                    help="compact neighbour lists of this many entries in all "
+                         "(pbf_initialize_compact) instead of max-neighbors slots per particle")
     ap.add_argument("--max-neighbors", type=int, default=256,
                     help="neighbour list capacity (the reference fixes 256)")
     args = ap.parse_args()
@@ -616,7 +619,7 @@ def main():
     n = len(pos)
 
     s = pkg.PBFSolver(local)
-    s.initialize(n, mn, mx, prm, args.max_neighbors)
+    s.initialize(n, mn, mx, prm, args.max_neighbors, list_capacity=args.list_capacity)
     for k, fn in (("spheres", s.set_spheres), ("boxes", s.set_boxes), ("planes", s.set_planes)):
         if col.get(k):
             fn(col[k])
@@ -701,6 +704,8 @@ def main():
             "config": {"workload": WORKLOAD if args.scene == "dam_break_1m" else args.scene,
                        "particles": n, "iterations": prm.solverIterations,
                        "max_neighbors": args.max_neighbors,
+                       "neighbor_lists": ("compact, %d entries" % args.list_capacity
+                                          if args.list_capacity else "slot-major"),
                        "substeps": prm.substeps, "parallelism": "replicas" if world > 1 else
                        "single GPU", "l2": "step working set ~250 MB > 129 MB L2 (no flush)",
                        "timing": "CUDA events around %d graph-replayed steps on the solver "

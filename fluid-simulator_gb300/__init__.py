@@ -167,6 +167,7 @@ def _declare(L):
         "pbf_last_error": ([_vp], C.c_char_p),
         "pbf_initialize": ([_vp, sz, F3, F3, C.POINTER(_Params)], S),
         "pbf_initialize_ex": ([_vp, sz, F3, F3, C.POINTER(_Params), C.c_int], S),
+        "pbf_initialize_compact": ([_vp, sz, F3, F3, C.POINTER(_Params), C.c_int, sz], S),
         "pbf_set_particles": ([_vp, _vp, _vp, sz], S),
         "pbf_set_particles_device": ([_vp, _vp, _vp, sz], S),
         "pbf_set_spheres": ([_vp, _vp, sz], S),
@@ -341,9 +342,16 @@ class PBFSolver:
 
     # -- reference API -------------------------------------------------------
     def initialize(self, max_particles: int, min_bounds, max_bounds, params: SimulationParams,
-                   max_neighbors: int = 256):
+                   max_neighbors: int = 256, list_capacity: Optional[int] = None):
+        """PBFSolver::initialize.  list_capacity: compact neighbour lists of
+        that many entries in all (pbf_initialize_compact) instead of
+        max_neighbors slots per particle."""
         self._params = params.to_struct()
-        if max_neighbors == 256:
+        if list_capacity is not None:
+            st = self._L.pbf_initialize_compact(self._h, int(max_particles), _f3(min_bounds),
+                                                _f3(max_bounds), C.byref(self._params),
+                                                int(max_neighbors), int(list_capacity))
+        elif max_neighbors == 256:
             st = self._L.pbf_initialize(self._h, int(max_particles), _f3(min_bounds),
                                         _f3(max_bounds), C.byref(self._params))
         else:

@@ -50,6 +50,14 @@ __device__ __forceinline__ const SceneConst& scene_of(const StepConst& c, int i)
     return c.scenes[__ldg(&c.sid[i])];
 }
 
+// First entry and entry stride of particle i's neighbour list.
+__device__ __forceinline__ size_t nb_first(const StepConst& c, int i) {
+    return c.nb_off ? static_cast<size_t>(__ldg(&c.nb_off[i])) : static_cast<size_t>(i);
+}
+__device__ __forceinline__ size_t nb_step(const StepConst& c) {
+    return c.nb_off ? size_t(1) : c.stride;
+}
+
 // Grid and first global cell key of slot i: the scene's (B) or c.g.
 template <bool B>
 __device__ __forceinline__ void grid_of(const StepConst& c, int i, GridConst& g, uint32_t& base) {
@@ -255,7 +263,8 @@ __device__ __forceinline__ float lambda_finish(const StepConst& c, const LambdaA
 
 // The neighbour walk of particle i (position pi): writes the list slot-major
 // at out[slot * stride] (at most max_nb entries) and returns the full count.
-template <bool B>
+// STORE = false counts the hits without writing the list.
+template <bool B, bool STORE = true>
 __device__ __forceinline__ int walk(const StepConst& c, int i, float4 pi,
                                     const float* __restrict__ sx, const float* __restrict__ sy,
                                     const float* __restrict__ sz, const int* __restrict__ first,
@@ -275,7 +284,7 @@ __device__ __forceinline__ int walk(const StepConst& c, int i, float4 pi,
     const uint32_t gxy = gx * static_cast<uint32_t>(g.gy);
     const float h2 = c.k.h2;
     const int max_nb = c.max_nb;
-    const size_t stride = c.stride;
+    const size_t stride = nb_step(c);
     const f32x2 px = pack2(pi.x, pi.x), py = pack2(pi.y, pi.y), pz = pack2(pi.z, pi.z);
     int count = 0;
     // Rows z -> y; inside a row the cells x0..x1 are consecutive keys, so the
@@ -315,12 +324,17 @@ __device__ __forceinline__ int walk(const StepConst& c, int i, float4 pi,
                 const int self = i - j0;
                 if (self >= 0 && self < 32) valid &= ~(1u << self);
                 mask &= valid;
-                while (mask) {
-                    const int b = __ffs(mask) - 1;
-                    mask &= mask - 1u;
-                    if (count < max_nb)
-                        out[static_cast<size_t>(count) * stride] = static_cast<uint32_t>(j0 + b);
-                    ++count;
+                if constexpr (STORE) {
+                    while (mask) {
+                        const int b = __ffs(mask) - 1;
+                        mask &= mask - 1u;
+                        if (count < max_nb)
+                            out[static_cast<size_t>(count) * stride] =
+                                static_cast<uint32_t>(j0 + b);
+                        ++count;
+                    }
+                } else {
+                    count += __popc(mask);
                 }
             }
         }
@@ -337,10 +351,10 @@ k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || fatal(status)) return;
     const float4 pi = xs[i];
-    uint32_t* __restrict__ out = nbr + i;
+    uint32_t* __restrict__ out = nbr + nb_first(c, i);
     const int count = walk<B>(c, i, pi, sx, sy, sz, first, out);
     const int max_nb = c.max_nb;
-    const size_t stride = c.stride;
+    const size_t stride = nb_step(c);
     const f32x2 px = pack2(pi.x, pi.x), py = pack2(pi.y, pi.y), pz = pack2(pi.z, pi.z);
     cnt[i] = count;
     if (count > max_nb) atomicOr(status, kStatusNeighborOverflow);
@@ -386,6 +400,115 @@ k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
         } else {
             lam[i] = lambda_finish(c, acc);
         }
+    }
+}
+
+// Compact lists, first pass: the walk's neighbour count only.
+template <bool B>
+__global__ void __launch_bounds__(kMaxTunedBlock)
+k_count(const float4* __restrict__ xs, const float* __restrict__ sx,
+        const float* __restrict__ sy, const float* __restrict__ sz,
+        const int* __restrict__ first, StepConst c, int n, int* __restrict__ cnt,
+        unsigned* __restrict__ status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || fatal(status)) return;
+    const int count = walk<B, false>(c, i, xs[i], sx, sy, sz, first, nullptr);
+    cnt[i] = count;
+    if (count > c.max_nb) atomicOr(status, kStatusNeighborOverflow);
+}
+
+// Exclusive scan of the counts into list offsets, in three launches: tile
+// scans with tile totals, a scan of the totals, and the carry-in.  64-bit
+// sums; offsets are 32-bit because the list capacity is below 2^32.
+constexpr int kScanThreads = 256, kScanItems = 8, kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ unsigned long long block_scan_u64(unsigned long long v,
+                                                             unsigned long long* warp_tot,
+                                                             unsigned long long& total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) warp_tot[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x / 32;
+        unsigned long long w = lane < nw ? warp_tot[lane] : 0ull;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += t;
+        }
+        if (lane < nw) warp_tot[lane] = w;
+    }
+    __syncthreads();
+    total = warp_tot[blockDim.x / 32 - 1];
+    const unsigned long long before = warp ? warp_tot[warp - 1] : 0ull;
+    __syncthreads();
+    return before + incl - v;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+k_nb_scan_tiles(const int* __restrict__ cnt, int n, uint32_t* __restrict__ off,
+                unsigned long long* __restrict__ tile_sum, const unsigned* __restrict__ status) {
+    if (fatal(status)) return;
+    __shared__ unsigned long long warp_tot[kScanThreads / 32];
+    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    unsigned long long v[kScanItems], sum = 0;
+#pragma unroll
+    for (int r = 0; r < kScanItems; ++r) {
+        const int idx = base + r;
+        v[r] = idx < n ? static_cast<unsigned long long>(max(0, cnt[idx])) : 0ull;
+        sum += v[r];
+    }
+    unsigned long long total;
+    unsigned long long run = block_scan_u64(sum, warp_tot, total);
+#pragma unroll
+    for (int r = 0; r < kScanItems; ++r) {
+        const int idx = base + r;
+        // Tile-local; a clamped value means a total of at least 2^32 entries,
+        // above any capacity, which the last launch flags.
+        if (idx < n) off[idx] = static_cast<uint32_t>(min(run, 0xffffffffull));
+        run += v[r];
+    }
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+}
+
+// One block: exclusive scan of the tile totals in place.
+__global__ void __launch_bounds__(kScanThreads)
+k_nb_scan_sums(unsigned long long* __restrict__ tile_sum, int tiles,
+               const unsigned* __restrict__ status) {
+    if (fatal(status)) return;
+    __shared__ unsigned long long warp_tot[kScanThreads / 32];
+    unsigned long long carry = 0;
+    for (int t0 = 0; t0 < tiles; t0 += kScanThreads) {
+        const int t = t0 + threadIdx.x;
+        const unsigned long long v = t < tiles ? tile_sum[t] : 0ull;
+        unsigned long long total;
+        const unsigned long long ex = block_scan_u64(v, warp_tot, total);
+        if (t < tiles) tile_sum[t] = carry + ex;
+        carry += total;
+    }
+    if (threadIdx.x == 0) tile_sum[tiles] = carry;
+}
+
+// Carry-in, the total at off[n], and the capacity check.
+__global__ void __launch_bounds__(kScanThreads)
+k_nb_scan_add(int n, size_t cap, const unsigned long long* __restrict__ tile_sum, int tiles,
+              uint32_t* __restrict__ off, unsigned* __restrict__ status) {
+    if (fatal(status)) return;
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned long long total = tile_sum[tiles];
+    if (idx < n) {
+        const unsigned long long o = tile_sum[idx / kScanTile] + off[idx];
+        off[idx] = static_cast<uint32_t>(min(o, 0xffffffffull));
+    }
+    if (idx == 0) {
+        off[n] = static_cast<uint32_t>(min(total, 0xffffffffull));
+        if (total > cap) atomicOr(status, kStatusListOverflow);
     }
 }
 
@@ -501,7 +624,7 @@ __device__ __forceinline__ void delta_sum(const StepConst& c, const float4* __re
     const float li = lam[i];
     float ax = 0.0f, ay = 0.0f, az = 0.0f;
     for_each_neighbor_pair<PosLam>(
-        nbr + i, c.stride, count,
+        nbr + nb_first(c, i), nb_step(c), count,
         [&](uint32_t j) { return PosLam{__ldg(&xs[j]), __ldg(&lam[j])}; },
         [&](const PosLam& a, const PosLam& b) {
             delta_term2<N>(c, pi, li, a.p, a.l, b.p, b.l, ax, ay, az);
@@ -583,7 +706,7 @@ __device__ __forceinline__ float4 xsph_one(const StepConst& c, const float4* __r
     const float4 pi = x[i];
     float cx = 0.0f, cy = 0.0f, cz = 0.0f;
     for_each_neighbor_pair<PosVel>(
-        nbr + i, c.stride, count,
+        nbr + nb_first(c, i), nb_step(c), count,
         [&](uint32_t j) { return PosVel{__ldg(&x[j]), __ldg(&v[j])}; },
         [&](const PosVel& a, const PosVel& b) {
             float w0, w1, x0, x1, y0, y1, z0, z1;
@@ -637,7 +760,7 @@ k_search_xsph(const float4* __restrict__ xs, const float* __restrict__ sx,
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || fatal(status)) return;
     const float4 pi = xs[i];
-    const int count = walk<B>(c, i, pi, sx, sy, sz, first, nbr + i);
+    const int count = walk<B>(c, i, pi, sx, sy, sz, first, nbr + nb_first(c, i));
     cnt[i] = count;
     if (count > c.max_nb) atomicOr(status, kStatusNeighborOverflow);
     float4 out = xsph_one(c, xs, v, nbr, count, i, B ? scene_of(c, i).xsph_c : c.xsph_c);
@@ -663,7 +786,7 @@ k_vorticity(const float4* __restrict__ x, const float4* __restrict__ v,
     const float4 pi = x[i], vi = v[i];
     float ox = 0.0f, oy = 0.0f, oz = 0.0f;
     for_each_neighbor_pair<PosVel>(
-        nbr + i, c.stride, count,
+        nbr + nb_first(c, i), nb_step(c), count,
         [&](uint32_t j) { return PosVel{__ldg(&x[j]), __ldg(&v[j])}; },
         [&](const PosVel& a, const PosVel& b) {
             const f32x2 dx = diff2(pi.x, a.p.x, b.p.x), dy = diff2(pi.y, a.p.y, b.p.y),
@@ -715,7 +838,7 @@ __device__ __forceinline__ float4 confine_one(const StepConst& c, const float4* 
     const float wil = wi.w;  // |omega_i|, stored by k_vorticity
     float ex = 0.0f, ey = 0.0f, ez = 0.0f;
     for_each_neighbor_pair<PosVel>(
-        nbr + i, c.stride, count,
+        nbr + nb_first(c, i), nb_step(c), count,
         [&](uint32_t j) { return PosVel{__ldg(&x[j]), __ldg(&om[j])}; },
         [&](const PosVel& a, const PosVel& b) {
             const f32x2 dx = diff2(pi.x, a.p.x, b.p.x), dy = diff2(pi.y, a.p.y, b.p.y),
@@ -802,8 +925,10 @@ k_density(const float4* __restrict__ x, const uint32_t* __restrict__ nbr,
     const float4 pi = x[i];
     const int count = min(cnt[i], c.max_nb);
     float wsum = c.k.c_poly6;
+    const uint32_t* list = nbr + nb_first(c, i);
+    const size_t step = nb_step(c);
     for (int k = 0; k < count; ++k) {
-        const float4 pj = __ldg(&x[__ldg(&nbr[static_cast<size_t>(k) * c.stride + i])]);
+        const float4 pj = __ldg(&x[__ldg(&list[static_cast<size_t>(k) * step])]);
         wsum = fadd(wsum, poly6(c.k, dist2(fsub(pi.x, pj.x), fsub(pi.y, pj.y), fsub(pi.z, pj.z))));
     }
     const float mass = c.scenes ? scene_of(c, i).mass : c.mass;
@@ -947,6 +1072,33 @@ void launch_search_xsph(const float4* xs, const float* sx, const float* sy, cons
     else
         launch_k(k_search_xsph<false>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr, cnt, v, v_out,
                  vin, resolve, status);
+}
+
+void launch_count(const float4* xs, const float* sx, const float* sy, const float* sz,
+                  const int* first, const StepConst& c, int n, int* cnt, unsigned* status,
+                  cudaStream_t st) {
+    const int bs = tuned_block(c, kTunedSearch);
+    const unsigned g = blocks_for(n, bs);
+    if (c.scenes)
+        launch_k(k_count<true>, g, bs, st, xs, sx, sy, sz, first, c, n, cnt, status);
+    else
+        launch_k(k_count<false>, g, bs, st, xs, sx, sy, sz, first, c, n, cnt, status);
+}
+
+size_t nb_scan_scratch_words(size_t n) {
+    const size_t tiles = (n + kScanTile - 1) / kScanTile;
+    return 2 * (tiles + 1);  // 64-bit tile sums and the total
+}
+
+void launch_nb_scan(const int* cnt, uint32_t* off, size_t cap, int n, uint32_t* scratch,
+                    unsigned* status, cudaStream_t st) {
+    const int tiles = static_cast<int>((static_cast<size_t>(n) + kScanTile - 1) / kScanTile);
+    auto* sums = reinterpret_cast<unsigned long long*>(scratch);
+    launch_k(k_nb_scan_tiles, static_cast<unsigned>(std::max(tiles, 1)), kScanThreads, st, cnt,
+             n, off, sums, status);
+    launch_k(k_nb_scan_sums, 1u, kScanThreads, st, sums, tiles, status);
+    launch_k(k_nb_scan_add, blocks_for(std::max(n, 1), kScanThreads), kScanThreads, st, n, cap,
+             sums, tiles, off, status);
 }
 
 template <bool B>

@@ -39,6 +39,10 @@ struct StepConst {
     const uint16_t* sid;
     // Threads per block of the tuned kernels (TunedKernel order); 0 = kBlock.
     int blk[6];
+    // Compact neighbour lists: particle i's list is nbr[nb_off[i] + k] inside
+    // nb_cap entries.  Null: slot-major lists, nbr[k * stride + i].
+    const uint32_t* nb_off;
+    size_t nb_cap;
 };
 
 // Kernels whose block size the solver's autotuner chooses.
@@ -98,6 +102,15 @@ void launch_search_xsph(const float4* xs, const float* sx, const float* sy, cons
 void launch_delta_apply(const float4* xs, const uint32_t* nbr, const int* cnt, const float* lam,
                         const StepConst& c, int n, float4* xs_out, uint32_t* keys_out,
                         unsigned* status, cudaStream_t st, uint8_t* moved = nullptr);
+// Compact lists: neighbour counts of the walk (no list written), then the
+// exclusive scan of the counts into off (n + 1 entries; a total above cap
+// sets kStatusListOverflow).  scratch: nb_scan_scratch_words(n) words.
+void launch_count(const float4* xs, const float* sx, const float* sy, const float* sz,
+                  const int* first, const StepConst& c, int n, int* cnt, unsigned* status,
+                  cudaStream_t st);
+size_t nb_scan_scratch_words(size_t n);
+void launch_nb_scan(const int* cnt, uint32_t* off, size_t cap, int n, uint32_t* scratch,
+                    unsigned* status, cudaStream_t st);
 // id_new may be null (ids not carried).
 void launch_finalize(const uint32_t* org, const float4* x_old, const float4* vin_old,
                      const float4* v_old, const uint32_t* id_old, const float4* xs, int n,

@@ -25,7 +25,8 @@ constexpr float kProjectionTolScale = 9.5367431640625e-07f;  // 8 * FLT_EPSILON 
 enum StatusBits : unsigned {
     kStatusNeighborOverflow = 1u << 0,
     kStatusNotConverged = 1u << 1,
-    kStatusFatalMask = kStatusNeighborOverflow | kStatusNotConverged,
+    kStatusListOverflow = 1u << 2,  // compact lists: total count over capacity
+    kStatusFatalMask = kStatusNeighborOverflow | kStatusNotConverged | kStatusListOverflow,
 };
 
 __device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }

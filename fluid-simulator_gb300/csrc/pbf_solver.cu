@@ -164,6 +164,13 @@ struct pbf_solver {
     // Threads per block of the tuned kernels (0 = the default 256).
     int tuned[kTunedCount] = {};
 
+    // Compact neighbour lists (list_cap > 0): every rebuild counts the
+    // neighbours, scans the counts into nb_off and writes each particle's
+    // list contiguously into list_cap entries in all.  0: slot-major lists of
+    // max_nb slots per particle.
+    size_t list_cap = 0;
+    DeviceBuffer nb_off, nb_scratch;
+
     // Device state.
     DeviceBuffer f4[kF4Pool];
     DeviceBuffer ids[2], org[2];
@@ -257,6 +264,10 @@ struct pbf_solver {
             c.sid = scene_id.as<uint16_t>();
         }
         for (int k = 0; k < kTunedCount; ++k) c.blk[k] = tuned[k];
+        if (list_cap > 0) {
+            c.nb_off = nb_off.as<uint32_t>();
+            c.nb_cap = list_cap;
+        }
         return c;
     }
 
@@ -326,9 +337,20 @@ struct pbf_solver {
                 cur = nxt;
                 org_cur = org_next;
             };
+            // Compact lists: neighbour counts and their scan before each walk
+            // that writes lists.
+            auto count_and_scan = [&](int xs) {
+                if (list_cap == 0) return;
+                launch_count(P(xs), soa.as<float>(), soa.as<float>() + soa_stride(),
+                             soa.as<float>() + 2 * soa_stride(), cell_first.as<int>(), c, N,
+                             cnt.as<int>(), sp, st);
+                launch_nb_scan(cnt.as<int>(), nb_off.as<uint32_t>(), list_cap, N,
+                               nb_scratch.as<uint32_t>(), sp, st);
+            };
             for (int it = 0; it < prm.solverIterations; ++it) {
                 rebuild();
                 M(kStSearchLambda);
+                count_and_scan(cur);
                 launch_search(P(cur), soa.as<float>(), soa.as<float>() + soa_stride(),
                               soa.as<float>() + 2 * soa_stride(), cell_first.as<int>(), c, N,
                               nbr.as<uint32_t>(), cnt.as<int>(), lam.as<float>(), sp, true, st);
@@ -362,6 +384,7 @@ struct pbf_solver {
             if (xsph) {
                 const int t = take();
                 M(kStSearch);
+                count_and_scan(rx);
                 launch_search_xsph(P(rx), soa.as<float>(), soa.as<float>() + soa_stride(),
                                    soa.as<float>() + 2 * soa_stride(), cell_first.as<int>(), c,
                                    N, nbr.as<uint32_t>(), cnt.as<int>(), P(rv), P(t), P(vin2),
@@ -370,6 +393,7 @@ struct pbf_solver {
                 rv = t;
             } else if (vort) {
                 M(kStSearch);
+                count_and_scan(rx);
                 launch_search(P(rx), soa.as<float>(), soa.as<float>() + soa_stride(),
                               soa.as<float>() + 2 * soa_stride(), cell_first.as<int>(), c, N,
                               nbr.as<uint32_t>(), cnt.as<int>(), nullptr, sp, false, st);
@@ -541,6 +565,8 @@ struct pbf_solver {
         if (s & kStatusNeighborOverflow)
             fail(PBF_ERR_OVERFLOW, "Particle neighbor count exceeds solver capacity");
         if (s & kStatusNotConverged) fail(PBF_ERR_RUNTIME, "Collision constraints did not converge");
+        if (s & kStatusListOverflow)
+            fail(PBF_ERR_OVERFLOW, "Neighbor lists exceed the compact list capacity");
     }
 
     void run_frames(size_t frames, bool sync) {
@@ -553,11 +579,14 @@ struct pbf_solver {
     }
 
     // ---- API ------------------------------------------------------------------
+    // lcap > 0: compact neighbour lists of lcap entries in all.
     void initialize(size_t max_particles, pbf_float3 lo, pbf_float3 hi, const pbf_params& p,
-                    int maxnb) {
+                    int maxnb, size_t lcap = 0) {
         if (max_particles == 0)
             fail(PBF_ERR_INVALID_ARGUMENT, "maxParticles must be greater than zero");
         if (maxnb <= 0) fail(PBF_ERR_INVALID_ARGUMENT, "maxNeighbors must be greater than zero");
+        if (lcap > 0xffffffffull)
+            fail(PBF_ERR_LENGTH, "Compact neighbor list capacity exceeds 2^32 - 1 entries");
         if (max_particles > std::numeric_limits<size_t>::max() / size_t(maxnb))
             fail(PBF_ERR_LENGTH, "Neighbor buffer size overflows size_t");
         if (max_particles > static_cast<size_t>(std::numeric_limits<int>::max()))
@@ -576,7 +605,8 @@ struct pbf_solver {
         const uint64_t ncells = uint64_t(d[0]) * uint64_t(d[1]) * uint64_t(d[2]);
 
         use_device();
-        allocate_and_commit(max_particles, strd, maxnb, ncells, DeviceBuffer(), DeviceBuffer(), {});
+        allocate_and_commit(max_particles, strd, maxnb, ncells, DeviceBuffer(), DeviceBuffer(), {},
+                            lcap);
         prm = p;
         mn = lo;
         mx = hi;
@@ -587,7 +617,8 @@ struct pbf_solver {
     // cells, then makes it (and the scene table, empty for one scene) the
     // active configuration.  Nothing changes if an allocation fails.
     void allocate_and_commit(size_t max_particles, size_t strd, int maxnb, uint64_t ncells,
-                             DeviceBuffer ntab, DeviceBuffer nsid, std::vector<size_t> off) {
+                             DeviceBuffer ntab, DeviceBuffer nsid, std::vector<size_t> off,
+                             size_t lcap = 0) {
         const size_t f4b = max_particles * sizeof(float4);
         const size_t u4b = max_particles * sizeof(uint32_t);
         DeviceBuffer nf4[kF4Pool], nids[2], norg[2];
@@ -597,7 +628,12 @@ struct pbf_solver {
         DeviceBuffer nkeys(u4b), nskeys(u4b), nsidx(u4b), nakeys(u4b), naidx(u4b);
         DeviceBuffer nfirst((ncells + 1) * sizeof(int));
         DeviceBuffer nsoa(3 * ((max_particles + 1 + 63) / 64 * 64) * sizeof(float));
-        DeviceBuffer nnbr(strd * size_t(maxnb) * sizeof(uint32_t));
+        DeviceBuffer nnbr((lcap > 0 ? lcap : strd * size_t(maxnb)) * sizeof(uint32_t));
+        DeviceBuffer nnboff, nnbscr;
+        if (lcap > 0) {
+            nnboff.allocate((max_particles + 1) * sizeof(uint32_t));
+            nnbscr.allocate(nb_scan_scratch_words(max_particles) * sizeof(uint32_t));
+        }
         DeviceBuffer ncnt(u4b), nlam(u4b), nscr(sort_scratch_bytes(int(max_particles)));
         DeviceBuffer nstat(sizeof(unsigned)), ntmp(f4b), nftmp(u4b);
 
@@ -615,6 +651,9 @@ struct pbf_solver {
         cell_first = std::move(nfirst);
         soa = std::move(nsoa);
         nbr = std::move(nnbr);
+        nb_off = std::move(nnboff);
+        nb_scratch = std::move(nnbscr);
+        list_cap = lcap;
         cnt = std::move(ncnt);
         lam = std::move(nlam);
         sort_scratch = std::move(nscr);
@@ -917,6 +956,17 @@ pbf_status pbf_initialize_ex(pbf_solver* s, size_t max_particles, pbf_float3 lo,
     PBF_GUARD(s, {
         if (!p) fail(PBF_ERR_INVALID_ARGUMENT, "params must not be null");
         s->initialize(max_particles, lo, hi, *p, max_neighbors);
+    });
+}
+
+pbf_status pbf_initialize_compact(pbf_solver* s, size_t max_particles, pbf_float3 lo,
+                                  pbf_float3 hi, const pbf_params* p, int max_neighbors,
+                                  size_t list_capacity) {
+    PBF_GUARD(s, {
+        if (!p) fail(PBF_ERR_INVALID_ARGUMENT, "params must not be null");
+        if (list_capacity == 0)
+            fail(PBF_ERR_INVALID_ARGUMENT, "compact neighbor list capacity must be positive");
+        s->initialize(max_particles, lo, hi, *p, max_neighbors, list_capacity);
     });
 }
 

@@ -85,6 +85,17 @@ pbf_status pbf_initialize_ex(pbf_solver* s, size_t max_particles, pbf_float3 min
                              pbf_float3 max_bounds, const pbf_params* params,
                              int max_neighbors);
 
+/* Same with compact neighbour lists: each rebuild counts every particle's
+ * neighbours, scans the counts and stores each list contiguously, list_capacity
+ * entries in all (memory follows the actual neighbour count instead of
+ * max_particles x max_neighbors).  Results equal those of the slot-major lists
+ * bit for bit.  A step whose lists need more than list_capacity entries fails
+ * with PBF_ERR_OVERFLOW; max_neighbors still bounds each particle's count as in
+ * the reference.  list_capacity must be in [1, 2^32 - 1]. */
+pbf_status pbf_initialize_compact(pbf_solver* s, size_t max_particles, pbf_float3 min_bounds,
+                                  pbf_float3 max_bounds, const pbf_params* params,
+                                  int max_neighbors, size_t list_capacity);
+
 /* PBFSolver::setParticles (src/pbf/pbf_solver.cu:118-152): host arrays,
  * finiteness checked, stable ids reset to the given order. */
 pbf_status pbf_set_particles(pbf_solver* s, const pbf_float4* positions,

@@ -90,6 +90,19 @@ def test_invalid_capacity_and_bounds(pbf):
         s.initialize(8, (0, 0, 0), (1e20, 2, 2), SP(**P(particleRadius=0.1)))
 
 
+def test_invalid_compact_list_capacity(pbf):
+    SP = pbf.SimulationParams
+    s = pbf.PBFSolver()
+    with pytest.raises(pbf.InvalidArgument):
+        s.initialize(8, (0, 0, 0), (1, 1, 1), SP(**P()), list_capacity=0)
+    with pytest.raises(pbf.LengthError):
+        s.initialize(8, (0, 0, 0), (1, 1, 1), SP(**P()), list_capacity=2 ** 32)
+    with pytest.raises(pbf.InvalidArgument):
+        s.initialize(8, (0, 0, 0), (1, 1, 1), SP(**P()), max_neighbors=0, list_capacity=64)
+    with pytest.raises(pbf.InvalidArgument):  # validation still runs first
+        s.initialize(8, (0, 0, 0), (1, 1, 1), SP(**P(dt=0.0)), list_capacity=64)
+
+
 INVALID = [
     dict(dt=0.0), dict(dt=math.nan), dict(dt=1.4e-45, substeps=2),
     dict(restDensity=-1.0), dict(restDensity=math.inf),
