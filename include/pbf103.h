@@ -171,13 +171,15 @@ pbf_status pbf_block_sizes(const pbf_solver* s, int* sizes, int count);
  * xsphViscosity.  The differentiated step is integration, the density
  * constraint iterations with s_corr and the container clamp, the velocity
  * update, XSPH and the container velocity response, over neighbour lists
- * recorded by the forward (integer data, not differentiated); it runs the
- * same arithmetic as PBFSolver::step in particle-id order (sums in another
- * order, so it agrees with pbf_step to rounding).  One substep per step, no
- * vorticity confinement, no sphere/box/plane colliders.  The forward keeps
- * (x, v) every `checkpoint_every` steps; the backward recomputes each
- * segment from its checkpoint.  State and gradient pointers may be host or
- * device memory.  Gradient arrays are float4 with w ignored. */
+ * recorded by the forward (integer data, not differentiated).  The forward
+ * runs the solver's own kernels: one step from a state in particle-id order
+ * is bit for bit pbf_step on that state, and every step returns to
+ * particle-id order, so forward(x, v, a + b) equals forward(forward(x, v, a),
+ * b).  One substep per step, no vorticity confinement, no sphere/box/plane
+ * colliders.  The forward keeps (x, v) every `checkpoint_every` steps and
+ * records its last segment; the backward recomputes each earlier segment
+ * from its checkpoint.  State and gradient pointers may be host or device
+ * memory.  Gradient arrays are float4 with w ignored. */
 typedef struct pbf_adjoint pbf_adjoint;
 pbf_status pbf_adjoint_create(pbf_adjoint** out, int device);
 void pbf_adjoint_destroy(pbf_adjoint* a);
