@@ -665,7 +665,8 @@ class PBFAdjoint:
 
     ``forward`` runs the differentiated step (integration, density
     constraint with s_corr and the container clamp, velocity update, XSPH,
-    container velocity response) from (x0, v0), keeping checkpoints;
+    vorticity confinement, container velocity response) from (x0, v0),
+    keeping checkpoints;
     ``backward`` takes dL/dx, dL/dv of that forward's final state and returns
     dL/dx0, dL/dv0, dL/drestDensity and dL/dxsphViscosity.  Arrays are (n, 4)
     float32 numpy arrays or contiguous CUDA tensors (anything with a

@@ -2,8 +2,8 @@
 // loss on the final particle state with respect to the initial positions and
 // velocities, the rest density and the XSPH strength.
 //
-// Differentiated step (one substep; container walls only; no vorticity
-// confinement):
+// Differentiated substep (container walls only; a step of S substeps is S
+// of them with dt / S, each taped as one step):
 //   integrate   v1 = v + g dt, p0 = x + v1 dt               (integration.cu:6-32)
 //   I times     lambda_i = -C_i / (gs^2 (S2_i + |G_i|^2) + eps),
 //               q = p + gs sum_j (lambda_i + lambda_j + s_corr) grad W_ij,
@@ -11,6 +11,9 @@
 //               (pbf_solver_kernels.cu:26-193, collision_kernels.cu:47-82)
 //   velocity    v2 = (p_I - x) / dt                         (pbf_solver_kernels.cu:195-211)
 //   XSPH        v3 = v2 + c sum_j (v2_j - v2_i) W_ij        (pbf_solver_kernels.cu:213-266)
+//   vorticity   v5 = v3 + dt eps (N x w), w_i = sum_j grad W_ij x (v3_j - v3_i),
+//               N = eta / |eta|, eta_i = sum_j (|w_j| - |w_i|) grad W_ij
+//               (pbf_solver_kernels.cu:268-385; only when eps != 0)
 //   response    v4 = wall contacts against v1 (restitution, friction)
 //               (collision_kernels.cu:236-276)
 // gs = m / rho0, C_i = rho_i / rho0 - 1, rho_i = m (W(0) + sum_j W_ij),
@@ -65,6 +68,9 @@ __device__ __forceinline__ float3 operator*(float s, float3 a) {
     return make_float3(s * a.x, s * a.y, s * a.z);
 }
 __device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float3 cross3(float3 a, float3 b) {
+    return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
 
 // Analytic derivatives used by the adjoint.  With rr = |r|:
 //   spiky gradient g(r) = f(rr) r,  f = c_spiky (1 - rr/h)^2 / rr
@@ -213,12 +219,14 @@ __device__ __forceinline__ float4 unmoved(uint8_t m, float3 g) {
 //   dL/dc += gv3_i . sum_j (v2_j - v2_i) W_ij
 //   gq_{I-1} at slot rel[s] of the last iteration's order = gp_F where the
 //   projection left the component unchanged, 0 elsewhere.
+// gx_vort (optional): position gradient from the vorticity confinement.
 template <int L>
 __global__ void k_xsph_adj(const float4* __restrict__ pF, const float4* __restrict__ v2,
                            const float4* __restrict__ gv3, const uint32_t* __restrict__ nbr,
                            const int* __restrict__ cnt, const float4* __restrict__ gx_next,
                            const uint32_t* __restrict__ org, const uint32_t* __restrict__ rel,
-                           const uint8_t* __restrict__ moved_last, StepConst c, int n,
+                           const uint8_t* __restrict__ moved_last,
+                           const float4* __restrict__ gx_vort, StepConst c, int n,
                            float4* __restrict__ gxs, float4* __restrict__ gq,
                            double* __restrict__ acc_c) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -246,7 +254,8 @@ __global__ void k_xsph_adj(const float4* __restrict__ pF, const float4* __restri
     acc_c[i] += static_cast<double>(dot3(gi, sv));
     const uint32_t o = org[i], r = rel[i];
     if (o >= static_cast<uint32_t>(n) || r >= static_cast<uint32_t>(n)) return;
-    const float3 gp = f3(gx_next[o]) + c.inv_dt * gv2 + c.xsph_c * pos;
+    float3 gp = f3(gx_next[o]) + c.inv_dt * gv2 + c.xsph_c * pos;
+    if (gx_vort) gp = gp + f3(gx_vort[i]);  // vorticity confinement's position terms
     gxs[o] = make_float4(-c.inv_dt * gv2.x, -c.inv_dt * gv2.y, -c.inv_dt * gv2.z, 0.0f);
     gq[r] = unmoved(moved_last[r], gp);
 }
@@ -360,6 +369,117 @@ __global__ void k_iter_adj_b(const float4* __restrict__ p, const float4* __restr
     }
 }
 
+// Vorticity confinement adjoint (computeVorticity, applyVorticityConfinement,
+// pbf_solver_kernels.cu:268-385), in the final sorted order.  Forward, with
+// g_kj the spiky gradient at x_k - x_j and v the velocities after XSPH:
+//   w_k = sum_j g_kj x (v_j - v_k),  m_k = |w_k|,
+//   eta_k = sum_j (m_j - m_k) g_kj,  N_k = eta_k / |eta_k| (0 when |eta_k| <= 1e-6),
+//   v'_k = v_k + dt eps (N_k x w_k).
+// First pass (a = dt eps gv'_k): gN = w x a, geta = (gN - N (N . gN)) / |eta|,
+// and the direct part of gw = a x N.
+template <int L>
+__global__ void k_conf_adj_a(const float4* __restrict__ pF, const float4* __restrict__ om,
+                             const uint32_t* __restrict__ nbr, const int* __restrict__ cnt,
+                             const float4* __restrict__ gv5, StepConst c, int n,
+                             float4* __restrict__ geta, float4* __restrict__ gw_direct) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = tid / L, lane = tid % L;
+    const bool live = i < n;
+    const int ii = live ? i : 0;
+    const float3 pi = f3(pF[ii]);
+    const float mi = om[ii].w;
+    const int count = live ? min(cnt[i], c.max_nb) : 0;
+    float3 eta = make_float3(0.0f, 0.0f, 0.0f);
+    for (int k = lane; k < count; k += L) {
+        const uint32_t j = __ldg(&nbr[static_cast<size_t>(k) * c.stride + i]);
+        const PairTerms t = pair_terms(c, pi - f3(__ldg(&pF[j])));
+        eta = eta + (__ldg(&om[j]).w - mi) * t.g;
+    }
+    eta = lane_sum<L>(eta);
+    if (!live || lane != 0) return;
+    const float3 w = f3(om[i]);
+    const float3 a = (c.dt * c.vort_eps) * f3(gv5[i]);
+    const float len = sqrtf(dot3(eta, eta));
+    float3 N = make_float3(0.0f, 0.0f, 0.0f), ge = N;
+    if (len > kEtaEpsilon) {
+        N = (1.0f / len) * eta;
+        const float3 gN = cross3(w, a);
+        ge = (1.0f / len) * (gN - dot3(N, gN) * N);
+    }
+    geta[i] = make_float4(ge.x, ge.y, ge.z, 0.0f);
+    const float3 gw = cross3(a, N);
+    gw_direct[i] = make_float4(gw.x, gw.y, gw.z, 0.0f);
+}
+
+// Second pass: the magnitude terms of eta,
+//   gm_k = -sum_j (geta_k + geta_j) . g_kj,
+//   gx_k = sum_j (m_j - m_k) H_kj (geta_k + geta_j),
+// and gw_k = direct + gm_k w_k / m_k.
+template <int L>
+__global__ void k_conf_adj_b(const float4* __restrict__ pF, const float4* __restrict__ om,
+                             const uint32_t* __restrict__ nbr, const int* __restrict__ cnt,
+                             const float4* __restrict__ geta,
+                             const float4* __restrict__ gw_direct, StepConst c, int n,
+                             float4* __restrict__ gw, float4* __restrict__ gx) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = tid / L, lane = tid % L;
+    const bool live = i < n;
+    const int ii = live ? i : 0;
+    const float3 pi = f3(pF[ii]), gei = f3(geta[ii]);
+    const float mi = om[ii].w;
+    const int count = live ? min(cnt[i], c.max_nb) : 0;
+    float gm = 0.0f;
+    float3 pos = make_float3(0.0f, 0.0f, 0.0f);
+    for (int k = lane; k < count; k += L) {
+        const uint32_t j = __ldg(&nbr[static_cast<size_t>(k) * c.stride + i]);
+        const float3 r = pi - f3(__ldg(&pF[j]));
+        const PairTerms t = pair_terms(c, r);
+        const float3 sg = gei + f3(__ldg(&geta[j]));
+        gm -= dot3(sg, t.g);
+        pos = pos + (__ldg(&om[j]).w - mi) * hess(t, r, sg);
+    }
+    gm = lane_sum<L>(gm);
+    pos = lane_sum<L>(pos);
+    if (!live || lane != 0) return;
+    float3 g = f3(gw_direct[i]);
+    if (mi > 0.0f) g = g + (gm / mi) * f3(om[i]);
+    gw[i] = make_float4(g.x, g.y, g.z, 0.0f);
+    gx[i] = make_float4(pos.x, pos.y, pos.z, 0.0f);
+}
+
+// Third pass: the vorticity sum,
+//   gv_k = gv'_k - sum_j (gw_k + gw_j) x g_kj,
+//   gx_k += sum_j H_kj ((v_j - v_k) x (gw_k + gw_j)).
+template <int L>
+__global__ void k_vort_adj(const float4* __restrict__ pF, const float4* __restrict__ v3,
+                           const uint32_t* __restrict__ nbr, const int* __restrict__ cnt,
+                           const float4* __restrict__ gw, const float4* __restrict__ gv5,
+                           StepConst c, int n, float4* __restrict__ gv3,
+                           float4* __restrict__ gx) {
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = tid / L, lane = tid % L;
+    const bool live = i < n;
+    const int ii = live ? i : 0;
+    const float3 pi = f3(pF[ii]), vi = f3(v3[ii]), gwi = f3(gw[ii]);
+    const int count = live ? min(cnt[i], c.max_nb) : 0;
+    float3 acc = make_float3(0.0f, 0.0f, 0.0f), pos = acc;
+    for (int k = lane; k < count; k += L) {
+        const uint32_t j = __ldg(&nbr[static_cast<size_t>(k) * c.stride + i]);
+        const float3 r = pi - f3(__ldg(&pF[j]));
+        const PairTerms t = pair_terms(c, r);
+        const float3 sg = gwi + f3(__ldg(&gw[j]));
+        acc = acc + cross3(sg, t.g);
+        pos = pos + hess(t, r, cross3(f3(__ldg(&v3[j])) - vi, sg));
+    }
+    acc = lane_sum<L>(acc);
+    pos = lane_sum<L>(pos);
+    if (!live || lane != 0) return;
+    const float3 g = f3(gv5[i]) - acc;
+    gv3[i] = make_float4(g.x, g.y, g.z, 0.0f);
+    const float4 x0 = gx[i];
+    gx[i] = make_float4(x0.x + pos.x, x0.y + pos.y, x0.z + pos.z, 0.0f);
+}
+
 // Contact response of the forward (resolveVelocitiesKernel, the solver's
 // arithmetic), with positions and velocities stored back in particle-id order.
 __global__ void k_respond_out(const float4* __restrict__ pF, const float4* __restrict__ vinF,
@@ -402,7 +522,7 @@ struct pbf_adjoint {
     std::string last_error;
 
     size_t n = 0, stride = 0;
-    int max_nb = 128, every = 10, iters = 0;
+    int max_nb = 128, every = 10, iters = 0, subs = 1;
     int steps_done = 0;
     pbf_params prm{};
     uint64_t cells = 0;
@@ -422,8 +542,10 @@ struct pbf_adjoint {
     // The tape holds the last segment of the latest forward (recorded by the
     // forward itself, so the backward need not recompute it).
     bool tape_last = false;
-    // Adjoint work arrays.
+    // Adjoint work arrays (gva..gvx: vorticity confinement only).
     DeviceBuffer gx, gv, gxs, gv1, gv3, gq0, gq1, gpart, aux, aa, acc_r, acc_c;
+    DeviceBuffer gva, gvb, gvc, gvx;
+    bool vort = false;  // vorticity confinement in the step
     // Captured segments: (kind, length, parity) -> graph.
     std::map<std::tuple<int, int, int>, cudaGraphExec_t> graphs;
 
@@ -440,11 +562,13 @@ struct pbf_adjoint {
     // Tape of step slot t.  float4 arrays: P(t, k) positions of sort k in its
     // order (k = 0..I; k = I is the final sort, i.e. the step's new
     // positions), then v2 (entering XSPH), v1 in the final order (entering
-    // the contacts) and v3 (leaving XSPH).  uint32 arrays: REL(t, k) the
+    // the contacts) and v3 (leaving XSPH); with vorticity confinement also
+    // the vorticity (w = |w|) and v5 (leaving the confinement, entering the
+    // contacts).  uint32 arrays: REL(t, k) the
     // permutation of sort k (its slot s takes slot REL[s] of the previous
     // order; for k = 0 that order is particle-id order), and ORG(t) the
     // composed permutation of the final order (slot -> particle id).
-    int f4_per_step() const { return iters + 4; }
+    int f4_per_step() const { return iters + (vort ? 6 : 4); }
     int u32_per_step() const { return iters + 2; }
     float4* P(int t, int k) {
         return tf4.as<float4>() + (static_cast<size_t>(t) * f4_per_step() + k) * n;
@@ -452,6 +576,10 @@ struct pbf_adjoint {
     float4* V2(int t) { return P(t, iters + 1); }
     float4* VINF(int t) { return P(t, iters + 2); }
     float4* V3(int t) { return P(t, iters + 3); }
+    float4* OM(int t) { return P(t, iters + 4); }
+    float4* V5(int t) { return P(t, iters + 5); }
+    // Velocities entering the contact response.
+    float4* VC(int t) { return vort ? V5(t) : V3(t); }
     uint32_t* REL(int t, int k) {
         return tu32.as<uint32_t>() + (static_cast<size_t>(t) * u32_per_step() + k) * n;
     }
@@ -473,12 +601,9 @@ struct pbf_adjoint {
             fail(PBF_ERR_LENGTH, "Particle count exceeds CUDA kernel index range");
         if (maxnb <= 0) fail(PBF_ERR_INVALID_ARGUMENT, "maxNeighbors must be greater than zero");
         if (ckpt_every <= 0) fail(PBF_ERR_INVALID_ARGUMENT, "checkpoint interval must be positive");
-        if (p.substeps != 1) fail(PBF_ERR_INVALID_ARGUMENT, "the adjoint takes one substep per step");
-        if (p.vorticityStrength != 0.0f)
-            fail(PBF_ERR_INVALID_ARGUMENT,
-                 "the adjoint covers integration, the density constraint, container contacts "
-                 "and XSPH; vorticityStrength must be 0");
         validate_params(p);
+        if (static_cast<long long>(ckpt_every) * p.substeps > std::numeric_limits<int>::max())
+            fail(PBF_ERR_LENGTH, "checkpoint interval times substeps exceeds the int range");
         const double width = double(hi.x) - double(lo.x);
         const double depth = double(hi.z) - double(lo.z);
         if (width < 2.0 * double(p.particleRadius) || depth < 2.0 * double(p.particleRadius))
@@ -489,8 +614,10 @@ struct pbf_adjoint {
         clear_graphs();
         n = count;
         max_nb = maxnb;
-        every = ckpt_every;
+        subs = p.substeps;
+        every = ckpt_every * subs;  // in substeps: each substep is one taped step
         iters = p.solverIterations;
+        vort = p.vorticityStrength != 0.0f;
         prm = p;
         stride = (n + 255) / 256 * 256;
         cells = uint64_t(d[0]) * uint64_t(d[1]) * uint64_t(d[2]);
@@ -513,7 +640,7 @@ struct pbf_adjoint {
         c.lambda_eps = p.lambdaEpsilon;
         c.gs = p.particleMass / p.restDensity;
         c.gs2 = c.gs * c.gs;
-        c.dt = p.dt;
+        c.dt = p.dt / static_cast<float>(p.substeps);  // as the solver forms it
         c.inv_dt = 1.0f / c.dt;
         c.gravx = p.gravity.x;
         c.gravy = p.gravity.y;
@@ -522,7 +649,7 @@ struct pbf_adjoint {
         c.restitution = p.collisionRestitution;
         c.friction = p.collisionFriction;
         c.xsph_c = p.xsphViscosity;
-        c.vort_eps = 0.0f;
+        c.vort_eps = p.vorticityStrength;
         c.max_nb = max_nb;
         c.stride = stride;
         c.col.cminx = lo.x;
@@ -553,6 +680,12 @@ struct pbf_adjoint {
         states.allocate((E + 1) * 2 * f4b);
         for (DeviceBuffer* b : {&gx, &gv, &gxs, &gv1, &gv3, &gq0, &gq1, &gpart, &aux})
             b->allocate(f4b);
+        for (DeviceBuffer* b : {&gva, &gvb, &gvc, &gvx}) {
+            if (vort)
+                b->allocate(f4b);
+            else
+                *b = DeviceBuffer();
+        }
         aa.allocate(n * sizeof(float));
         acc_r.allocate(n * sizeof(double));
         acc_c.allocate(n * sizeof(double));
@@ -627,7 +760,12 @@ struct pbf_adjoint {
                         nullptr, sp, stream);
         launch_search_xsph(pF, s0, s0 + soa_stride(), s0 + 2 * soa_stride(), first.as<int>(), c, N,
                            NB(t, I), CN(t, I), V2(t), V3(t), VINF(t), false, sp, stream);
-        adj::k_respond_out<<<adj::grid(N), adj::kB, 0, stream>>>(pF, VINF(t), V3(t), ORG(t), c, N,
+        if (vort) {
+            launch_vorticity(pF, V3(t), NB(t, I), CN(t, I), c, N, OM(t), true, sp, stream);
+            launch_confine(pF, NB(t, I), CN(t, I), OM(t), V3(t), c, N, V5(t), VINF(t), false, sp,
+                           stream);
+        }
+        adj::k_respond_out<<<adj::grid(N), adj::kB, 0, stream>>>(pF, VINF(t), VC(t), ORG(t), c, N,
                                                                  x_out, v_out);
         cuda_check(cudaGetLastError());
     }
@@ -648,13 +786,31 @@ struct pbf_adjoint {
         const unsigned gl = adj::grid_lanes(N, L);
         float4* pF = P(t, I);
         adj::k_respond_adj<<<adj::grid(N), adj::kB, 0, stream>>>(
-            pF, VINF(t), V3(t), gv.as<float4>(), ORG(t), c, N, gv3.as<float4>(),
+            pF, VINF(t), VC(t), gv.as<float4>(), ORG(t), c, N, gv3.as<float4>(),
             gv1.as<float4>());
+        // gv3 holds the gradient of the velocities entering the contacts; with
+        // vorticity confinement its three passes turn that into the gradient
+        // of the XSPH output (gvb) plus position terms (gvx).
+        const float4* g_xsph_out = gv3.as<float4>();
+        const float4* gx_vort = nullptr;
+        if (vort) {
+            adj::k_conf_adj_a<L><<<gl, adj::kB, 0, stream>>>(
+                pF, OM(t), NB(t, I), CN(t, I), gv3.as<float4>(), c, N, gva.as<float4>(),
+                gvb.as<float4>());
+            adj::k_conf_adj_b<L><<<gl, adj::kB, 0, stream>>>(
+                pF, OM(t), NB(t, I), CN(t, I), gva.as<float4>(), gvb.as<float4>(), c, N,
+                gvc.as<float4>(), gvx.as<float4>());
+            adj::k_vort_adj<L><<<gl, adj::kB, 0, stream>>>(
+                pF, V3(t), NB(t, I), CN(t, I), gvc.as<float4>(), gv3.as<float4>(), c, N,
+                gvb.as<float4>(), gvx.as<float4>());
+            g_xsph_out = gvb.as<float4>();
+            gx_vort = gvx.as<float4>();
+        }
         float4* gqa = gq0.as<float4>();
         float4* gqb = gq1.as<float4>();
         adj::k_xsph_adj<L><<<gl, adj::kB, 0, stream>>>(
-            pF, V2(t), gv3.as<float4>(), NB(t, I), CN(t, I), gx.as<float4>(), ORG(t), REL(t, I),
-            MV(t, I - 1), c, N, gxs.as<float4>(), gqa, acc_c.as<double>());
+            pF, V2(t), g_xsph_out, NB(t, I), CN(t, I), gx.as<float4>(), ORG(t), REL(t, I),
+            MV(t, I - 1), gx_vort, c, N, gxs.as<float4>(), gqa, acc_c.as<double>());
         for (int k = I - 1; k >= 0; --k) {
             adj::k_iter_adj_a<L><<<gl, adj::kB, 0, stream>>>(
                 P(t, k), LAM(t, k), gqa, NB(t, k), CN(t, k), c, N, gpart.as<float4>(),
@@ -701,10 +857,14 @@ struct pbf_adjoint {
             fail(PBF_ERR_OVERFLOW, "Particle neighbor count exceeds solver capacity");
     }
 
-    void forward(const pbf_float4* x0, const pbf_float4* v0, int steps, pbf_float4* x_out,
+    // `frames` solver steps of `subs` substeps each.
+    void forward(const pbf_float4* x0, const pbf_float4* v0, int frames, pbf_float4* x_out,
                  pbf_float4* v_out) {
         if (n == 0) fail(PBF_ERR_LOGIC, "the adjoint must be initialized before the forward");
-        if (steps < 0) fail(PBF_ERR_INVALID_ARGUMENT, "step count must not be negative");
+        if (frames < 0) fail(PBF_ERR_INVALID_ARGUMENT, "step count must not be negative");
+        if (static_cast<long long>(frames) * subs > std::numeric_limits<int>::max())
+            fail(PBF_ERR_LENGTH, "step count times substeps exceeds the int range");
+        const int steps = frames * subs;  // substeps, one taped step each
         if (!x0 || !v0 || !x_out || !v_out) fail(PBF_ERR_INVALID_ARGUMENT, "null state pointer");
         cuda_check(cudaSetDevice(device));
         const size_t f4b = n * sizeof(float4);

@@ -170,13 +170,14 @@ pbf_status pbf_block_sizes(const pbf_solver* s, int* sizes, int count);
  * the initial positions and velocities, restDensity (mass held fixed) and
  * xsphViscosity.  The differentiated step is integration, the density
  * constraint iterations with s_corr and the container clamp, the velocity
- * update, XSPH and the container velocity response, over neighbour lists
+ * update, XSPH, vorticity confinement and the container velocity response,
+ * over neighbour lists
  * recorded by the forward (integer data, not differentiated).  The forward
- * runs the solver's own kernels: one step from a state in particle-id order
- * is bit for bit pbf_step on that state, and every step returns to
- * particle-id order, so forward(x, v, a + b) equals forward(forward(x, v, a),
- * b).  One substep per step, no vorticity confinement, no sphere/box/plane
- * colliders.  The forward keeps (x, v) every `checkpoint_every` steps and
+ * runs the solver's own kernels: with one substep, one step from a state in
+ * particle-id order is bit for bit pbf_step on that state; every substep
+ * returns to particle-id order, so forward(x, v, a + b) equals
+ * forward(forward(x, v, a), b).  A step of S substeps is taped as S substeps
+ * of dt / S (checkpoint_every counts steps).  No sphere/box/plane colliders.  The forward keeps (x, v) every `checkpoint_every` steps and
  * records its last segment; the backward recomputes each earlier segment
  * from its checkpoint.  State and gradient pointers may be host or device
  * memory.  Gradient arrays are float4 with w ignored. */

@@ -4,7 +4,7 @@
 // forward-mode gradient runs it with them).
 //
 // One step, in the reference's formulas evaluated in double
-// (include/pbf/sph_helpers.cuh:13-95, src/pbf/pbf_solver_kernels.cu:26-266,
+// (include/pbf/sph_helpers.cuh:13-95, src/pbf/pbf_solver_kernels.cu:26-385,
 // src/pbf/collision_kernels.cu:21-82,236-276, src/pbf/pbf_solver.cu:198-325):
 //   v1 = v + g dt, p = x + v1 dt
 //   I times: neighbours of p (|p_i - p_j|^2 <= h^2, j != i),
@@ -12,6 +12,8 @@
 //            lambda_i = -C_i / (gs^2 (sum |g_ij|^2 + |sum g_ij|^2) + eps),
 //            p_i <- clamp(p_i + gs sum (lambda_i + lambda_j + s_corr_ij) g_ij)
 //   neighbours of p; v2 = (p - x) / dt; v3 = v2 + c sum (v2_j - v2_i) W_ij;
+//   with vorticity strength eps: w_i = sum g_ij x (v3_j - v3_i),
+//   eta_i = sum (|w_j| - |w_i|) g_ij, v3 <- v3 + dt eps (eta/|eta| x w_i);
 //   v4 = container contacts of v3 against v1 at p; x <- p, v <- v4.
 // Values are double; every quantity carries K tangents (Dual<K>), the
 // derivatives along K input directions of (x0, v0, rho0, c).  Neighbour sets,
@@ -79,6 +81,14 @@ template <int K> D3<K> operator+(const D3<K>& a, const D3<K>& b) { return {a.x +
 template <int K> D3<K> operator-(const D3<K>& a, const D3<K>& b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
 template <int K> D3<K> operator*(const Dual<K>& s, const D3<K>& a) { return {s * a.x, s * a.y, s * a.z}; }
 template <int K> Dual<K> dot(const D3<K>& a, const D3<K>& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+template <int K> D3<K> cross(const D3<K>& a, const D3<K>& b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+// |a|, with a zero derivative at a = 0 (where the norm has none).
+template <int K> Dual<K> norm3(const D3<K>& a) {
+    const Dual<K> q = dot(a, a);
+    return q.v > 0.0 ? dsqrt(q) : Dual<K>(0.0);
+}
 
 template <int K>
 struct Diff {
@@ -189,8 +199,15 @@ struct Diff {
         else if (pos.z.v >= maxZ - eps) contact(2, -1.0, vin, vv);
     }
 
+    // One frame: `substeps` substeps of dt / substeps (rounded to float as
+    // the solver forms it, src/pbf/pbf_solver.cu:193).
     void step() {
-        const Dual<K> dt(p.dt), m(p.particleMass), eps(p.lambdaEpsilon);
+        const float sub_dt = p.dt / float(p.substeps);
+        for (int k = 0; k < p.substeps; ++k) substep(double(sub_dt));
+    }
+
+    void substep(double dt_value) {
+        const Dual<K> dt(dt_value), m(p.particleMass), eps(p.lambdaEpsilon);
         const Dual<K> gs = m / rho0, gs2 = gs * gs;
         const D3<K> g{Dual<K>(p.gravity.x), Dual<K>(p.gravity.y), Dual<K>(p.gravity.z)};
         std::vector<D3<K>> v1(n), q(n), nq(n);
@@ -234,7 +251,7 @@ struct Diff {
             q.swap(nq);
         }
         lists(q);
-        std::vector<D3<K>> v2(n);
+        std::vector<D3<K>> v2(n), v3(n);
         for (size_t i = 0; i < n; ++i) v2[i] = Dual<K>(1.0) / dt * (q[i] - x[i]);
 #pragma omp parallel for schedule(dynamic, 256)
         for (long ii = 0; ii < long(n); ++ii) {
@@ -244,7 +261,44 @@ struct Diff {
                 const D3<K> r = q[i] - q[size_t(j)];
                 acc = acc + poly6(dot(r, r)) * (v2[size_t(j)] - v2[i]);
             }
-            D3<K> vv = v2[i] + xsph * acc;
+            v3[i] = v2[i] + xsph * acc;
+        }
+        if (p.vorticityStrength != 0.0f) {
+            // computeVorticity / applyVorticityConfinement
+            // (pbf_solver_kernels.cu:268-385): w_i = sum_j grad W_ij x (v_j - v_i),
+            // eta_i = sum_j (|w_j| - |w_i|) grad W_ij, v += dt eps (eta/|eta| x w_i).
+            std::vector<D3<K>> w(n);
+            std::vector<Dual<K>> mw(n);
+#pragma omp parallel for schedule(dynamic, 256)
+            for (long ii = 0; ii < long(n); ++ii) {
+                const size_t i = size_t(ii);
+                D3<K> acc{Dual<K>(0.0), Dual<K>(0.0), Dual<K>(0.0)};
+                for (int j : nb[i]) {
+                    const D3<K> r = q[i] - q[size_t(j)];
+                    acc = acc + cross(spiky(r, dot(r, r)), v3[size_t(j)] - v3[i]);
+                }
+                w[i] = acc;
+                mw[i] = norm3(acc);
+            }
+            const Dual<K> eps_v(double(p.vorticityStrength));
+            std::vector<D3<K>> v5(n);
+#pragma omp parallel for schedule(dynamic, 256)
+            for (long ii = 0; ii < long(n); ++ii) {
+                const size_t i = size_t(ii);
+                D3<K> eta{Dual<K>(0.0), Dual<K>(0.0), Dual<K>(0.0)};
+                for (int j : nb[i]) {
+                    const D3<K> r = q[i] - q[size_t(j)];
+                    eta = eta + (mw[size_t(j)] - mw[i]) * spiky(r, dot(r, r));
+                }
+                const Dual<K> le = norm3(eta);
+                D3<K> N{Dual<K>(0.0), Dual<K>(0.0), Dual<K>(0.0)};
+                if (le.v > 1.0e-6) N = (Dual<K>(1.0) / le) * eta;
+                v5[i] = v3[i] + (dt * eps_v) * cross(N, w[i]);
+            }
+            v3.swap(v5);
+        }
+        for (size_t i = 0; i < n; ++i) {
+            D3<K> vv = v3[i];
             respond(q[i], v1[i], vv);
             v[i] = vv;
         }
@@ -256,7 +310,7 @@ template <int K>
 int run(size_t n, const orc_float4* x0, const orc_float4* v0, const double* tx0,
         const double* tv0, const double* trho, const double* tc, int ntan, const orc_params* prm,
         orc_float3 lo, orc_float3 hi, int steps, const orc_float4* states, double* x_out,
-        double* v_out, double* tx_out, double* tv_out) {
+        double* v_out, double* tx_out, double* tv_out, const double* phys) {
     Diff<K> s;
     s.n = n;
     s.p = *prm;
@@ -269,8 +323,10 @@ int run(size_t n, const orc_float4* x0, const orc_float4* v0, const double* tx0,
     s.gx = dims[0];
     s.gy = dims[1];
     s.gz = dims[2];
-    s.rho0 = Dual<K>(prm->restDensity);
-    s.xsph = Dual<K>(prm->xsphViscosity);
+    // phys (optional): rest density and XSPH strength in double, so central
+    // differences may take steps below float32 resolution.
+    s.rho0 = Dual<K>(phys ? phys[0] : double(prm->restDensity));
+    s.xsph = Dual<K>(phys ? phys[1] : double(prm->xsphViscosity));
     for (int k = 0; k < ntan; ++k) {
         s.rho0.d[size_t(k)] = trho ? trho[k] : 0.0;
         s.xsph.d[size_t(k)] = tc ? tc[k] : 0.0;
@@ -339,20 +395,30 @@ int run(size_t n, const orc_float4* x0, const orc_float4* v0, const double* tx0,
 
 }  // namespace
 
+extern "C" int orc_diff_rollout_phys(size_t n, const orc_float4* x0, const orc_float4* v0,
+                                     const double* tx0, const double* tv0, const double* trho,
+                                     const double* tc, int ntan, const orc_params* prm,
+                                     orc_float3 lo, orc_float3 hi, int steps,
+                                     const orc_float4* states, double* x_out, double* v_out,
+                                     double* tx_out, double* tv_out, const double* phys) {
+    if (!prm || !x0 || !v0 || !x_out || !v_out || ntan < 0 || ntan > 12 || steps < 0)
+        return ORC_ERR_INVALID;
+    if (ntan == 0)
+        return run<0>(n, x0, v0, nullptr, nullptr, nullptr, nullptr, 0, prm, lo, hi, steps,
+                      states, x_out, v_out, nullptr, nullptr, phys);
+    if (ntan <= 4)
+        return run<4>(n, x0, v0, tx0, tv0, trho, tc, ntan, prm, lo, hi, steps, states, x_out,
+                      v_out, tx_out, tv_out, phys);
+    return run<12>(n, x0, v0, tx0, tv0, trho, tc, ntan, prm, lo, hi, steps, states, x_out, v_out,
+                   tx_out, tv_out, phys);
+}
+
 extern "C" int orc_diff_rollout(size_t n, const orc_float4* x0, const orc_float4* v0,
                                 const double* tx0, const double* tv0, const double* trho,
                                 const double* tc, int ntan, const orc_params* prm,
                                 orc_float3 lo, orc_float3 hi, int steps,
                                 const orc_float4* states, double* x_out, double* v_out,
                                 double* tx_out, double* tv_out) {
-    if (!prm || !x0 || !v0 || !x_out || !v_out || ntan < 0 || ntan > 12 || steps < 0)
-        return ORC_ERR_INVALID;
-    if (ntan == 0)
-        return run<0>(n, x0, v0, nullptr, nullptr, nullptr, nullptr, 0, prm, lo, hi, steps,
-                      states, x_out, v_out, nullptr, nullptr);
-    if (ntan <= 4)
-        return run<4>(n, x0, v0, tx0, tv0, trho, tc, ntan, prm, lo, hi, steps, states, x_out,
-                      v_out, tx_out, tv_out);
-    return run<12>(n, x0, v0, tx0, tv0, trho, tc, ntan, prm, lo, hi, steps, states, x_out, v_out,
-                   tx_out, tv_out);
+    return orc_diff_rollout_phys(n, x0, v0, tx0, tv0, trho, tc, ntan, prm, lo, hi, steps, states,
+                                 x_out, v_out, tx_out, tv_out, nullptr);
 }

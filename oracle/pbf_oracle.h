@@ -151,6 +151,13 @@ int orc_diff_rollout(size_t n, const orc_float4* x0, const orc_float4* v0, const
                      const orc_params* prm, orc_float3 lo, orc_float3 hi, int steps,
                      const orc_float4* states, double* x_out, double* v_out, double* tx_out,
                      double* tv_out);
+/* Same, with restDensity and xsphViscosity taken from phys[0], phys[1] in
+ * double instead of from params (phys may be NULL). */
+int orc_diff_rollout_phys(size_t n, const orc_float4* x0, const orc_float4* v0, const double* tx0,
+                          const double* tv0, const double* trho, const double* tc, int ntan,
+                          const orc_params* prm, orc_float3 lo, orc_float3 hi, int steps,
+                          const orc_float4* states, double* x_out, double* v_out, double* tx_out,
+                          double* tv_out, const double* phys);
 
 #ifdef __cplusplus
 }

@@ -1,9 +1,9 @@
 """The FP64 forward-mode restatement used to check the GPU adjoint
 (oracle/pbf_diff_oracle.cpp), pinned on the CPU:
 
-* its values follow the pinned FP64 oracle solver step for step (vorticity
-  off, one substep, container only), to FP64 rounding of a different
-  summation order;
+* its values follow the pinned FP64 oracle solver step for step (with and
+  without vorticity confinement, one or two substeps, container only), to
+  FP64 rounding of a different summation order;
 * its tangents equal central differences of its own values.
 """
 
@@ -11,16 +11,22 @@ import numpy as np
 import pytest
 
 
-def small_scene(scenes, nx=8, ny=8, nz=4):
+def small_scene(scenes, nx=8, ny=8, nz=4, vorticity=0.0, substeps=1):
     pos, vel, mn, mx, prm, _ = scenes.dam_break(nx, ny, nz, (2 * nx * 0.05, ny * 0.05 * 1.5,
                                                                 2 * nz * 0.05))
-    prm.vorticityStrength = 0.0
+    prm.vorticityStrength = vorticity
+    prm.substeps = substeps
     prm.xsphViscosity = 2e-5
     return pos, vel, mn, mx, prm
 
 
-def test_values_follow_the_fp64_oracle(orc, scenes):
-    pos, vel, mn, mx, prm = small_scene(scenes)
+# (vorticity strength, substeps)
+CASES = [(0.0, 1), (1e-3, 1), (1e-4, 2)]
+
+
+@pytest.mark.parametrize("vorticity,substeps", CASES)
+def test_values_follow_the_fp64_oracle(orc, scenes, vorticity, substeps):
+    pos, vel, mn, mx, prm = small_scene(scenes, vorticity=vorticity, substeps=substeps)
     x, v = orc.diff_rollout(pos, vel, prm.as_dict(), mn, mx, 5)
     s = orc.OracleSolver(64)
     s.initialize(len(pos), mn, mx, prm.as_dict())
@@ -32,8 +38,9 @@ def test_values_follow_the_fp64_oracle(orc, scenes):
     assert (np.abs(v - vp[:, :3]) <= np.spacing(np.abs(vp[:, :3])) + 1e-30).all()
 
 
-def test_tangents_equal_central_differences(orc, scenes):
-    pos, vel, mn, mx, prm = small_scene(scenes)
+@pytest.mark.parametrize("vorticity,substeps", CASES)
+def test_tangents_equal_central_differences(orc, scenes, vorticity, substeps):
+    pos, vel, mn, mx, prm = small_scene(scenes, vorticity=vorticity, substeps=substeps)
     rng = np.random.default_rng(3)
     n = len(pos)
     dv = rng.standard_normal((n, 3))

@@ -5,7 +5,8 @@ checked against the FP64 forward-mode gradient of the same steps
 (oracle/pbf_diff_oracle.cpp, pinned on the CPU against the FP64 oracle
 solver and its own central differences) and against FP64 central finite
 differences, along random directions in x0 and v0 and along rest density and
-XSPH strength.  Tolerance: 1e-3 relative.
+XSPH strength, with and without vorticity confinement.  Tolerance: 1e-3
+relative.
 
 Over a few steps the FP32 and FP64 trajectories agree to rounding and both
 references apply.  Over longer horizons the collapsing dam is chaotic (the
@@ -21,10 +22,13 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def scene(scenes, nx=16, ny=16, nz=8, seed=0):
+VORTICITY = [0.0, 1e-4]
+
+
+def scene(scenes, nx=16, ny=16, nz=8, seed=0, vorticity=0.0):
     box = (2 * nx * 0.05, ny * 0.05 * 1.5, 2 * nz * 0.05)
     pos, vel, mn, mx, prm, _ = scenes.dam_break(nx, ny, nz, box, seed=seed)
-    prm.vorticityStrength = 0.0
+    prm.vorticityStrength = vorticity
     prm.xsphViscosity = 2e-5
     rng = np.random.default_rng(seed + 1)
     target = pos[:, :3].astype(np.float64) + np.array([0.3, 0.0, 0.0])
@@ -50,8 +54,9 @@ def adjoint_grads(pbf, pos, vel, mn, mx, prm, target, steps, every):
     return x, L, gx0[:, :3].astype(np.float64), gv0[:, :3].astype(np.float64), gr, gc
 
 
-def test_taped_forward_follows_the_solver(pbf, scenes):
-    pos, vel, mn, mx, prm, _ = scene(scenes)
+@pytest.mark.parametrize("vorticity", VORTICITY)
+def test_taped_forward_follows_the_solver(pbf, scenes, vorticity):
+    pos, vel, mn, mx, prm, _ = scene(scenes, vorticity=vorticity)
     a = pbf.PBFAdjoint()
     a.initialize(len(pos), mn, mx, prm, max_neighbors=128, checkpoint_every=3)
     s = pbf.PBFSolver()
@@ -99,8 +104,9 @@ def test_backward_repeats_bit_for_bit(pbf, scenes):
     assert first[2] == second[2] and first[3] == second[3]
 
 
-def test_adjoint_matches_fp64_forward_mode_and_finite_differences(pbf, scenes, orc):
-    pos, vel, mn, mx, prm, target = scene(scenes)
+@pytest.mark.parametrize("vorticity", VORTICITY)
+def test_adjoint_matches_fp64_forward_mode_and_finite_differences(pbf, scenes, orc, vorticity):
+    pos, vel, mn, mx, prm, target = scene(scenes, vorticity=vorticity)
     steps, every = 6, 4  # two segments, the second shorter
     x, L, gx0, gv0, gr, gc = adjoint_grads(pbf, pos, vel, mn, mx, prm, target, steps, every)
     n = len(pos)
@@ -129,8 +135,8 @@ def test_adjoint_matches_fp64_forward_mode_and_finite_differences(pbf, scenes, o
     assert (rel <= 1e-3).all(), (adj, jvp, rel)
 
     # FP64 central differences along the first v0 direction and rest density.
-    def loss64(v0=vel, q=p):
-        xx, _ = orc.diff_rollout(pos, v0, q, mn, mx, steps)
+    def loss64(v0=vel, **phys):
+        xx, _ = orc.diff_rollout(pos, v0, p, mn, mx, steps, **phys)
         return float(((xx - target) ** 2).sum() / n)
 
     # A small step: larger ones cross the container clamps' kinks.
@@ -142,9 +148,11 @@ def test_adjoint_matches_fp64_forward_mode_and_finite_differences(pbf, scenes, o
     fd_v = (loss64(v0=vp) - loss64(v0=vm)) / (2 * e)
     adj_v = (gv0 * dvf).sum()
     assert abs(adj_v - fd_v) <= 1e-3 * abs(fd_v), (adj_v, fd_v)
-    r0 = p["restDensity"]
-    hi, lo = float(np.float32(r0 + 0.01)), float(np.float32(r0 - 0.01))
-    fd_r = (loss64(q=dict(p, restDensity=hi)) - loss64(q=dict(p, restDensity=lo))) / (hi - lo)
+    # The rest density is stepped in double: the loss is strongly curved where
+    # the confinement's |eta| is small, beyond float32-sized steps.
+    r0 = float(p["restDensity"])
+    hr = 1e-8 * r0
+    fd_r = (loss64(rest_density=r0 + hr) - loss64(rest_density=r0 - hr)) / (2 * hr)
     assert abs(gr - fd_r) <= 1e-3 * abs(fd_r), (gr, fd_r)
 
 
@@ -170,6 +178,30 @@ def test_autograd_function(pbf, scenes):
     assert abs(c.grad.item() - gc) <= 1e-6 * abs(gc)
 
 
+def test_adjoint_with_substeps_matches_fp64_forward_mode(pbf, scenes, orc):
+    # Two substeps per step: each substep is one taped step of dt / 2.
+    pos, vel, mn, mx, prm, target = scene(scenes, vorticity=1e-4)
+    prm.substeps = 2
+    steps, every = 4, 3  # two segments of 6 and 2 substeps
+    x, L, gx0, gv0, gr, gc = adjoint_grads(pbf, pos, vel, mn, mx, prm, target, steps, every)
+    n = len(pos)
+    rng = np.random.default_rng(17)
+    dirs = rng.standard_normal((2, n, 3))
+    k = 4
+    tv = np.zeros((k, n, 3))
+    tv[:2] = dirs
+    trho = np.array([0.0, 0.0, 1.0, 0.0])
+    tc = np.array([0.0, 0.0, 0.0, 1.0])
+    x64, _, txo, _ = orc.diff_rollout(pos, vel, prm.as_dict(), mn, mx, steps, tv0=tv,
+                                      trho=trho, tc=tc)
+    np.testing.assert_allclose(x[:, :3], x64, atol=5e-5, rtol=0)
+    d = (x64 - target) * (2.0 / n)
+    jvp = np.array([(d * txo[q]).sum() for q in range(k)])
+    adj = np.array([(gv0 * dirs[0]).sum(), (gv0 * dirs[1]).sum(), gr, gc])
+    rel = np.abs(adj - jvp) / np.abs(jvp)
+    assert (rel <= 1e-3).all(), (adj, jvp, rel)
+
+
 def gpu_states(a, pos, vel, steps):
     """(steps, 2, n, 4): x, v at the start of each step of the taped forward."""
     out = np.zeros((steps, 2, len(pos), 4), np.float32)
@@ -180,8 +212,9 @@ def gpu_states(a, pos, vel, steps):
     return out
 
 
-def test_adjoint_matches_fp64_tangents_along_its_trajectory(pbf, scenes, orc):
-    pos, vel, mn, mx, prm, target = scene(scenes)
+@pytest.mark.parametrize("vorticity", VORTICITY)
+def test_adjoint_matches_fp64_tangents_along_its_trajectory(pbf, scenes, orc, vorticity):
+    pos, vel, mn, mx, prm, target = scene(scenes, vorticity=vorticity)
     steps, every = 20, 7  # three segments, the last shorter
     n = len(pos)
     a = pbf.PBFAdjoint()
