@@ -76,6 +76,9 @@ def lib():
         L.orc_diff_rollout.restype = C.c_int
         L.orc_diff_rollout_phys.argtypes = L.orc_diff_rollout.argtypes + [_vp]
         L.orc_diff_rollout_phys.restype = C.c_int
+        L.orc_diff_rollout_col.argtypes = L.orc_diff_rollout_phys.argtypes + [
+            _vp, C.c_size_t, _vp, C.c_size_t, _vp, C.c_size_t]
+        L.orc_diff_rollout_col.restype = C.c_int
         L.orc_grid_dims.argtypes = [F3, F3, C.c_float, _i32p]
         L.orc_grid_dims.restype = C.c_int
         L.orc_grid_build.argtypes = [_vp, C.c_size_t, F3, C.c_float, _i32p, _vp, _vp, _vp, _vp]
@@ -543,15 +546,18 @@ class RefCudaSolver:
 
 
 def diff_rollout(x0, v0, params: dict, lo, hi, steps: int, tx0=None, tv0=None, trho=None,
-                 tc=None, states=None, rest_density=None, xsph=None):
+                 tc=None, states=None, rest_density=None, xsph=None, spheres=(), boxes=(),
+                 planes=()):
     """FP64 restatement of the differentiated step (pbf_diff_oracle.cpp).
 
     x0, v0: (n, 4) float32.  states: optional (steps, 2, n, 4) trajectory to
     linearise about (values restart from it at every step).  Tangents: tx0 /
     tv0 of shape (k, n, 3), trho / tc of shape (k,), k <= 12 directions.
     rest_density / xsph: optional double values replacing the params' float32
-    ones (central differences below float32 resolution).  Returns (x, v) as
-    (n, 3) float64 and, with tangents, their derivatives (k, n, 3)."""
+    ones (central differences below float32 resolution).  spheres / boxes /
+    planes: colliders as rows (cx, cy, cz, r) / (center, halfExtents) /
+    (point, normal).  Returns (x, v) as (n, 3) float64 and, with tangents,
+    their derivatives (k, n, 3)."""
     x0 = np.ascontiguousarray(x0, np.float32)
     v0 = np.ascontiguousarray(v0, np.float32)
     n = len(x0)
@@ -579,9 +585,11 @@ def diff_rollout(x0, v0, params: dict, lo, hi, steps: int, tx0=None, tv0=None, t
     if rest_density is not None or xsph is not None:
         phys = np.array([float(params["restDensity"]) if rest_density is None else rest_density,
                          float(params["xsphViscosity"]) if xsph is None else xsph], np.float64)
-    st = lib().orc_diff_rollout_phys(n, _p(x0), _p(v0), _p(tx0), _p(tv0), _p(trho), _p(tc), k,
-                                     C.byref(prm), f3(lo), f3(hi), int(steps), _p(states), _p(x),
-                                     _p(v), _p(tx), _p(tv), _p(phys))
+    sp, bx, pl = colliders_arrays(spheres, boxes, planes)
+    st = lib().orc_diff_rollout_col(n, _p(x0), _p(v0), _p(tx0), _p(tv0), _p(trho), _p(tc), k,
+                                    C.byref(prm), f3(lo), f3(hi), int(steps), _p(states), _p(x),
+                                    _p(v), _p(tx), _p(tv), _p(phys), _p(sp), sp.shape[0],
+                                    _p(bx), bx.shape[0], _p(pl), pl.shape[0])
     if st != ORC_OK:
         raise RuntimeError("orc_diff_rollout failed with status %d" % st)
     return (x, v, tx, tv) if k else (x, v)

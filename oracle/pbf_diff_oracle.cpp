@@ -21,6 +21,7 @@
 #include "pbf_oracle.h"
 
 #include <algorithm>
+#include <cfloat>
 #include <array>
 #include <cmath>
 #include <cstddef>
@@ -100,6 +101,7 @@ struct Diff {
     Dual<K> rho0, xsph;
     std::vector<D3<K>> x, v;
     std::vector<std::vector<int>> nb;
+    bool failed = false;  // a projection that did not converge
 
     void cell_of(double px, double py, double pz, int& cx, int& cy, int& cz) const {
         auto c1 = [&](double q, double m, int g) {
@@ -162,16 +164,129 @@ struct Diff {
         return Dual<K>(-double(p.scorrK)) * ipow(ratio * ratio * ratio, p.scorrN);
     }
 
-    void clamp(D3<K>& q) const {
+    // solveContainerKernel (collision_kernels.cu:47-82); true when moved.
+    bool clamp(D3<K>& q) const {
         const double r = p.particleRadius;
         const double minX = double(lo.x) + r, maxX = double(hi.x) - r;
         const double minY = double(lo.y) + r;
         const double minZ = double(lo.z) + r, maxZ = double(hi.z) - r;
-        if (q.x.v < minX) q.x = Dual<K>(minX);
-        if (q.x.v > maxX) q.x = Dual<K>(maxX);
-        if (q.y.v < minY) q.y = Dual<K>(minY);
-        if (q.z.v < minZ) q.z = Dual<K>(minZ);
-        if (q.z.v > maxZ) q.z = Dual<K>(maxZ);
+        bool mark = false;
+        auto lim = [&](Dual<K>& a, double v) { a = Dual<K>(v); mark = true; };
+        if (q.x.v < minX) lim(q.x, minX);
+        if (q.x.v > maxX) lim(q.x, maxX);
+        if (q.y.v < minY) lim(q.y, minY);
+        if (q.z.v < minZ) lim(q.z, minZ);
+        if (q.z.v > maxZ) lim(q.z, maxZ);
+        return mark;
+    }
+
+    // Sphere, box and plane colliders (collision_kernels.cu:84-234): the
+    // projections, decided on the values, carrying the tangents.
+    std::vector<orc_sphere> sph;
+    std::vector<orc_box> bxs;
+    std::vector<orc_plane> pls;
+
+    // projectionTolerance (collision_kernels.cu:9-14).
+    static double tol(const D3<K>& q, double ox, double oy, double oz, double rad) {
+        double t = std::fmax(rad, std::fmax(std::fabs(q.x.v), std::fabs(ox)));
+        t = std::fmax(t, std::fmax(std::fabs(q.y.v), std::fabs(oy)));
+        t = std::fmax(t, std::fmax(std::fabs(q.z.v), std::fabs(oz)));
+        return double(8.0f * FLT_EPSILON) * t;
+    }
+    // clamp of one coordinate into [lo, hi], keeping the tangent inside.
+    static Dual<K> clamp1(const Dual<K>& a, double lo_, double hi_) {
+        if (a.v < lo_) return Dual<K>(lo_);
+        if (a.v > hi_) return Dual<K>(hi_);
+        return a;
+    }
+    static void plane_unit(const orc_plane& pl, double& nx, double& ny, double& nz) {
+        const double nl = std::sqrt(double(pl.normal.x) * pl.normal.x +
+                                    double(pl.normal.y) * pl.normal.y +
+                                    double(pl.normal.z) * pl.normal.z);
+        nx = pl.normal.x / nl;
+        ny = pl.normal.y / nl;
+        nz = pl.normal.z / nl;
+    }
+    bool proj_spheres(D3<K>& q) const {
+        const double r = p.particleRadius;
+        bool mark = false;
+        for (const orc_sphere& sp : sph) {
+            const double cx = sp.center.x, cy = sp.center.y, cz = sp.center.z;
+            const double minD = double(sp.radius) + r;
+            const D3<K> o{q.x - Dual<K>(cx), q.y - Dual<K>(cy), q.z - Dual<K>(cz)};
+            const Dual<K> d2 = dot(o, o);
+            if (!(d2.v < minD * minD)) continue;
+            if (minD - std::sqrt(d2.v) <= tol(q, cx, cy, cz, minD)) continue;
+            mark = true;
+            if (d2.v == 0.0) {
+                q.x = Dual<K>(cx + minD);
+            } else {
+                const Dual<K> scale = Dual<K>(minD) / dsqrt(d2);
+                q = D3<K>{Dual<K>(cx), Dual<K>(cy), Dual<K>(cz)} + scale * o;
+            }
+        }
+        return mark;
+    }
+    bool proj_boxes(D3<K>& q) const {
+        const double r = p.particleRadius;
+        bool mark = false;
+        for (const orc_box& b : bxs) {
+            const double mnx = double(b.center.x) - b.halfExtents.x;
+            const double mny = double(b.center.y) - b.halfExtents.y;
+            const double mnz = double(b.center.z) - b.halfExtents.z;
+            const double mxx = double(b.center.x) + b.halfExtents.x;
+            const double mxy = double(b.center.y) + b.halfExtents.y;
+            const double mxz = double(b.center.z) + b.halfExtents.z;
+            const D3<K> cl{clamp1(q.x, mnx, mxx), clamp1(q.y, mny, mxy), clamp1(q.z, mnz, mxz)};
+            const D3<K> o = q - cl;
+            const Dual<K> d2 = dot(o, o);
+            if (d2.v > 0.0 && d2.v < r * r) {
+                if (r - std::sqrt(d2.v) <= tol(q, cl.x.v, cl.y.v, cl.z.v, r)) continue;
+                mark = true;
+                q = cl + (Dual<K>(r) / dsqrt(d2)) * o;
+            } else if (d2.v == 0.0) {
+                mark = true;
+                const double dX = std::fmin(q.x.v - mnx, mxx - q.x.v);
+                const double dY = std::fmin(q.y.v - mny, mxy - q.y.v);
+                const double dZ = std::fmin(q.z.v - mnz, mxz - q.z.v);
+                if (dX <= dY && dX <= dZ)
+                    q.x = Dual<K>(q.x.v - mnx < mxx - q.x.v ? mnx - r : mxx + r);
+                else if (dY <= dZ)
+                    q.y = Dual<K>(q.y.v - mny < mxy - q.y.v ? mny - r : mxy + r);
+                else
+                    q.z = Dual<K>(q.z.v - mnz < mxz - q.z.v ? mnz - r : mxz + r);
+            }
+        }
+        return mark;
+    }
+    bool proj_planes(D3<K>& q) const {
+        const double r = p.particleRadius;
+        bool mark = false;
+        for (const orc_plane& pl : pls) {
+            if (pl.normal.x == 0.0f && pl.normal.y == 0.0f && pl.normal.z == 0.0f) continue;
+            double nx, ny, nz;
+            plane_unit(pl, nx, ny, nz);
+            const D3<K> n{Dual<K>(nx), Dual<K>(ny), Dual<K>(nz)};
+            const D3<K> pt{Dual<K>(pl.point.x), Dual<K>(pl.point.y), Dual<K>(pl.point.z)};
+            const Dual<K> dist = dot(q - pt, n);
+            if (!(dist.v < r)) continue;
+            if (r - dist.v <= tol(q, pl.point.x, pl.point.y, pl.point.z, r)) continue;
+            mark = true;
+            q = q + (Dual<K>(r) - dist) * n;
+        }
+        return mark;
+    }
+    // CollisionSystem::solve per particle (collision_system.cu:133-172): to
+    // the fixed point, at most 32 passes; false when it did not converge.
+    bool project(D3<K>& q) const {
+        for (int pass = 0; pass < 32; ++pass) {
+            bool mark = clamp(q);
+            if (!sph.empty()) mark = proj_spheres(q) || mark;
+            if (!bxs.empty()) mark = proj_boxes(q) || mark;
+            if (!pls.empty()) mark = proj_planes(q) || mark;
+            if (!mark) return true;
+        }
+        return false;
     }
 
     // resolveContactVelocity for an axis normal (collision_kernels.cu:21-43).
@@ -187,8 +302,17 @@ struct Diff {
         for (int b = 0; b < 3; ++b)
             *c[b] = b == a ? Dual<K>(s) * target : ts * *c[b];
     }
+    // resolveContactVelocity against a unit normal n that may carry tangents.
+    void contact_n(const D3<K>& n, const D3<K>& vin, D3<K>& vv) const {
+        const Dual<K> vn = dot(vv, n), vinn = dot(vin, n);
+        const Dual<K> target =
+            vinn.v < 0.0 ? Dual<K>(-double(p.collisionRestitution)) * vinn : Dual<K>(0.0);
+        if (vn.v > target.v || (vn.v == target.v && vinn.v >= 0.0)) return;
+        const Dual<K> ts(1.0 - double(p.collisionFriction));
+        vv = ts * (vv - vn * n) + target * n;
+    }
     void respond(const D3<K>& pos, const D3<K>& vin, D3<K>& vv) const {
-        const double r = p.particleRadius, eps = 1e-4;
+        const double r = p.particleRadius, eps = double(1e-4f);  // kContactEpsilon
         const double minX = double(lo.x) + r, maxX = double(hi.x) - r;
         const double minY = double(lo.y) + r;
         const double minZ = double(lo.z) + r, maxZ = double(hi.z) - r;
@@ -197,6 +321,48 @@ struct Diff {
         if (pos.y.v <= minY + eps) contact(1, 1.0, vin, vv);
         if (pos.z.v <= minZ + eps) contact(2, 1.0, vin, vv);
         else if (pos.z.v >= maxZ - eps) contact(2, -1.0, vin, vv);
+        for (const orc_sphere& sp : sph) {
+            const double minD = double(sp.radius) + r;
+            const D3<K> o{pos.x - Dual<K>(sp.center.x), pos.y - Dual<K>(sp.center.y),
+                          pos.z - Dual<K>(sp.center.z)};
+            const Dual<K> d2 = dot(o, o);
+            const double cd = minD + eps;
+            if (d2.v > 0.0 && d2.v <= cd * cd) contact_n((Dual<K>(1.0) / dsqrt(d2)) * o, vin, vv);
+        }
+        for (const orc_box& b : bxs) {
+            const double mnx = double(b.center.x) - b.halfExtents.x;
+            const double mny = double(b.center.y) - b.halfExtents.y;
+            const double mnz = double(b.center.z) - b.halfExtents.z;
+            const double mxx = double(b.center.x) + b.halfExtents.x;
+            const double mxy = double(b.center.y) + b.halfExtents.y;
+            const double mxz = double(b.center.z) + b.halfExtents.z;
+            const D3<K> cl{clamp1(pos.x, mnx, mxx), clamp1(pos.y, mny, mxy),
+                           clamp1(pos.z, mnz, mxz)};
+            const D3<K> o = pos - cl;
+            const Dual<K> d2 = dot(o, o);
+            const double re = r + eps;
+            if (d2.v > 0.0 && d2.v <= re * re) {
+                contact_n((Dual<K>(1.0) / dsqrt(d2)) * o, vin, vv);
+            } else if (d2.v == 0.0) {
+                const double dX = std::fmin(pos.x.v - mnx, mxx - pos.x.v);
+                const double dY = std::fmin(pos.y.v - mny, mxy - pos.y.v);
+                const double dZ = std::fmin(pos.z.v - mnz, mxz - pos.z.v);
+                double n3[3] = {0.0, 0.0, 0.0};
+                if (dX <= dY && dX <= dZ) n3[0] = pos.x.v - mnx < mxx - pos.x.v ? -1.0 : 1.0;
+                else if (dY <= dZ) n3[1] = pos.y.v - mny < mxy - pos.y.v ? -1.0 : 1.0;
+                else n3[2] = pos.z.v - mnz < mxz - pos.z.v ? -1.0 : 1.0;
+                contact_n(D3<K>{Dual<K>(n3[0]), Dual<K>(n3[1]), Dual<K>(n3[2])}, vin, vv);
+            }
+        }
+        for (const orc_plane& pl : pls) {
+            if (pl.normal.x == 0.0f && pl.normal.y == 0.0f && pl.normal.z == 0.0f) continue;
+            double nx, ny, nz;
+            plane_unit(pl, nx, ny, nz);
+            const double dist = (pos.x.v - pl.point.x) * nx + (pos.y.v - pl.point.y) * ny +
+                                (pos.z.v - pl.point.z) * nz;
+            if (dist <= r + eps)
+                contact_n(D3<K>{Dual<K>(nx), Dual<K>(ny), Dual<K>(nz)}, vin, vv);
+        }
     }
 
     // One frame: `substeps` substeps of dt / substeps (rounded to float as
@@ -245,7 +411,7 @@ struct Diff {
                     acc = acc + (lam[i] + lam[size_t(j)] + scorr(d2)) * spiky(r, d2);
                 }
                 D3<K> np = q[i] + gs * acc;
-                clamp(np);
+                if (!project(np)) failed = true;
                 nq[i] = np;
             }
             q.swap(nq);
@@ -310,7 +476,9 @@ template <int K>
 int run(size_t n, const orc_float4* x0, const orc_float4* v0, const double* tx0,
         const double* tv0, const double* trho, const double* tc, int ntan, const orc_params* prm,
         orc_float3 lo, orc_float3 hi, int steps, const orc_float4* states, double* x_out,
-        double* v_out, double* tx_out, double* tv_out, const double* phys) {
+        double* v_out, double* tx_out, double* tv_out, const double* phys,
+        const orc_sphere* sp, size_t ns, const orc_box* bx, size_t nb, const orc_plane* pl,
+        size_t np) {
     Diff<K> s;
     s.n = n;
     s.p = *prm;
@@ -325,6 +493,9 @@ int run(size_t n, const orc_float4* x0, const orc_float4* v0, const double* tx0,
     s.gz = dims[2];
     // phys (optional): rest density and XSPH strength in double, so central
     // differences may take steps below float32 resolution.
+    if (sp) s.sph.assign(sp, sp + ns);
+    if (bx) s.bxs.assign(bx, bx + nb);
+    if (pl) s.pls.assign(pl, pl + np);
     s.rho0 = Dual<K>(phys ? phys[0] : double(prm->restDensity));
     s.xsph = Dual<K>(phys ? phys[1] : double(prm->xsphViscosity));
     for (int k = 0; k < ntan; ++k) {
@@ -366,6 +537,7 @@ int run(size_t n, const orc_float4* x0, const orc_float4* v0, const double* tx0,
             }
         }
         s.step();
+        if (s.failed) return ORC_ERR_NOT_CONVERGED;
     }
     for (size_t i = 0; i < n; ++i) {
         const D3<K>& a = s.x[i];
@@ -395,22 +567,36 @@ int run(size_t n, const orc_float4* x0, const orc_float4* v0, const double* tx0,
 
 }  // namespace
 
+extern "C" int orc_diff_rollout_col(size_t n, const orc_float4* x0, const orc_float4* v0,
+                                    const double* tx0, const double* tv0, const double* trho,
+                                    const double* tc, int ntan, const orc_params* prm,
+                                    orc_float3 lo, orc_float3 hi, int steps,
+                                    const orc_float4* states, double* x_out, double* v_out,
+                                    double* tx_out, double* tv_out, const double* phys,
+                                    const orc_sphere* sp, size_t ns, const orc_box* bx,
+                                    size_t nb, const orc_plane* pl, size_t np) {
+    if (!prm || !x0 || !v0 || !x_out || !v_out || ntan < 0 || ntan > 12 || steps < 0)
+        return ORC_ERR_INVALID;
+    if ((ns && !sp) || (nb && !bx) || (np && !pl)) return ORC_ERR_INVALID;
+    if (ntan == 0)
+        return run<0>(n, x0, v0, nullptr, nullptr, nullptr, nullptr, 0, prm, lo, hi, steps,
+                      states, x_out, v_out, nullptr, nullptr, phys, sp, ns, bx, nb, pl, np);
+    if (ntan <= 4)
+        return run<4>(n, x0, v0, tx0, tv0, trho, tc, ntan, prm, lo, hi, steps, states, x_out,
+                      v_out, tx_out, tv_out, phys, sp, ns, bx, nb, pl, np);
+    return run<12>(n, x0, v0, tx0, tv0, trho, tc, ntan, prm, lo, hi, steps, states, x_out, v_out,
+                   tx_out, tv_out, phys, sp, ns, bx, nb, pl, np);
+}
+
 extern "C" int orc_diff_rollout_phys(size_t n, const orc_float4* x0, const orc_float4* v0,
                                      const double* tx0, const double* tv0, const double* trho,
                                      const double* tc, int ntan, const orc_params* prm,
                                      orc_float3 lo, orc_float3 hi, int steps,
                                      const orc_float4* states, double* x_out, double* v_out,
                                      double* tx_out, double* tv_out, const double* phys) {
-    if (!prm || !x0 || !v0 || !x_out || !v_out || ntan < 0 || ntan > 12 || steps < 0)
-        return ORC_ERR_INVALID;
-    if (ntan == 0)
-        return run<0>(n, x0, v0, nullptr, nullptr, nullptr, nullptr, 0, prm, lo, hi, steps,
-                      states, x_out, v_out, nullptr, nullptr, phys);
-    if (ntan <= 4)
-        return run<4>(n, x0, v0, tx0, tv0, trho, tc, ntan, prm, lo, hi, steps, states, x_out,
-                      v_out, tx_out, tv_out, phys);
-    return run<12>(n, x0, v0, tx0, tv0, trho, tc, ntan, prm, lo, hi, steps, states, x_out, v_out,
-                   tx_out, tv_out, phys);
+    return orc_diff_rollout_col(n, x0, v0, tx0, tv0, trho, tc, ntan, prm, lo, hi, steps, states,
+                                x_out, v_out, tx_out, tv_out, phys, nullptr, 0, nullptr, 0,
+                                nullptr, 0);
 }
 
 extern "C" int orc_diff_rollout(size_t n, const orc_float4* x0, const orc_float4* v0,
@@ -419,6 +605,7 @@ extern "C" int orc_diff_rollout(size_t n, const orc_float4* x0, const orc_float4
                                 orc_float3 lo, orc_float3 hi, int steps,
                                 const orc_float4* states, double* x_out, double* v_out,
                                 double* tx_out, double* tv_out) {
-    return orc_diff_rollout_phys(n, x0, v0, tx0, tv0, trho, tc, ntan, prm, lo, hi, steps, states,
-                                 x_out, v_out, tx_out, tv_out, nullptr);
+    return orc_diff_rollout_col(n, x0, v0, tx0, tv0, trho, tc, ntan, prm, lo, hi, steps, states,
+                                x_out, v_out, tx_out, tv_out, nullptr, nullptr, 0, nullptr, 0,
+                                nullptr, 0);
 }

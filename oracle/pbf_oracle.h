@@ -158,6 +158,14 @@ int orc_diff_rollout_phys(size_t n, const orc_float4* x0, const orc_float4* v0, 
                           const orc_params* prm, orc_float3 lo, orc_float3 hi, int steps,
                           const orc_float4* states, double* x_out, double* v_out, double* tx_out,
                           double* tv_out, const double* phys);
+/* Same with sphere, box and plane colliders (projection and contact
+ * response); ORC_ERR_NOT_CONVERGED when a projection does not converge. */
+int orc_diff_rollout_col(size_t n, const orc_float4* x0, const orc_float4* v0, const double* tx0,
+                         const double* tv0, const double* trho, const double* tc, int ntan,
+                         const orc_params* prm, orc_float3 lo, orc_float3 hi, int steps,
+                         const orc_float4* states, double* x_out, double* v_out, double* tx_out,
+                         double* tv_out, const double* phys, const orc_sphere* sp, size_t ns,
+                         const orc_box* bx, size_t nb, const orc_plane* pl, size_t np);
 
 #ifdef __cplusplus
 }

@@ -84,3 +84,56 @@ def test_tangents_equal_central_differences(orc, scenes, vorticity, substeps):
     fdv = (x1 - x2) / (2 * e)
     _, _, txv, _ = orc.diff_rollout(pos, vel, p, mn, mx, steps, tv0=dvf[None])
     assert np.linalg.norm(fdv - txv[0]) <= 1e-4 * np.linalg.norm(txv[0])
+
+
+# Colliders inside and beside the small lattice (x in [0.025, 0.4], y in
+# [0.025, 0.4], z in [0.025, 0.2]): a sphere and a box in the fluid (particles
+# pushed out, the box's inside branch included) and a tilted floor plane.
+COLLIDERS = dict(spheres=[(0.1, 0.2, 0.1, 0.04)],
+                 boxes=[(0.3, 0.1, 0.1, 0.03, 0.03, 0.03)],
+                 planes=[(0.4, 0.03, 0.2) + tuple(np.array([0.2, 1.0, 0.0]) /
+                                                   np.linalg.norm([0.2, 1.0, 0.0]))])
+
+
+def test_values_with_colliders_follow_the_fp64_oracle(orc, scenes):
+    pos, vel, mn, mx, prm = small_scene(scenes, vorticity=1e-4)
+    x, v = orc.diff_rollout(pos, vel, prm.as_dict(), mn, mx, 5, **COLLIDERS)
+    s = orc.OracleSolver(64)
+    s.initialize(len(pos), mn, mx, prm.as_dict())
+    s.set_colliders(np.asarray(COLLIDERS["spheres"], np.float32),
+                    np.asarray(COLLIDERS["boxes"], np.float32),
+                    np.asarray(COLLIDERS["planes"], np.float32))
+    s.set_particles(pos, vel)
+    assert s.run(5) == 0
+    xp, vp = s.positions(), s.velocities()
+    # The colliders moved particles: the scene differs from the one without.
+    x0, _ = orc.diff_rollout(pos, vel, prm.as_dict(), mn, mx, 5)
+    assert np.abs(x - x0).max() > 1e-3
+    assert (np.abs(x - xp[:, :3]) <= np.spacing(np.abs(xp[:, :3]))).all()
+    assert (np.abs(v - vp[:, :3]) <= np.spacing(np.abs(vp[:, :3])) + 1e-30).all()
+
+
+def test_tangents_with_colliders_equal_central_differences(orc, scenes):
+    pos, vel, mn, mx, prm = small_scene(scenes, vorticity=1e-4)
+    p = prm.as_dict()
+    n = len(pos)
+    dv = np.random.default_rng(9).standard_normal((n, 3))
+    dv /= np.abs(dv).max()
+    steps = 4
+    e = 2.0 ** -24
+    vp, vm = vel.copy(), vel.copy()
+    vp[:, :3] += (e * dv).astype(np.float32)
+    vm[:, :3] -= (e * dv).astype(np.float32)
+    dvf = (vp[:, :3].astype(np.float64) - vm[:, :3].astype(np.float64)) / (2 * e)
+    x1, _ = orc.diff_rollout(pos, vp, p, mn, mx, steps, **COLLIDERS)
+    x2, _ = orc.diff_rollout(pos, vm, p, mn, mx, steps, **COLLIDERS)
+    fdv = (x1 - x2) / (2 * e)
+    _, _, txv, _ = orc.diff_rollout(pos, vel, p, mn, mx, steps, tv0=dvf[None], **COLLIDERS)
+    assert np.linalg.norm(fdv - txv[0]) <= 1e-4 * np.linalg.norm(txv[0])
+    r0 = float(p["restDensity"])
+    h = 1e-8 * r0
+    xa, _ = orc.diff_rollout(pos, vel, p, mn, mx, steps, rest_density=r0 + h, **COLLIDERS)
+    xb, _ = orc.diff_rollout(pos, vel, p, mn, mx, steps, rest_density=r0 - h, **COLLIDERS)
+    _, _, trx, _ = orc.diff_rollout(pos, vel, p, mn, mx, steps, trho=[1.0], **COLLIDERS)
+    fd = (xa - xb) / (2 * h)
+    assert np.linalg.norm(fd - trx[0]) <= 1e-4 * np.linalg.norm(trx[0])
