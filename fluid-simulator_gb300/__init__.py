@@ -197,6 +197,9 @@ def _declare(L):
         "pbf_adjoint_last_error": ([_vp], C.c_char_p),
         "pbf_adjoint_initialize": ([_vp, sz, F3, F3, C.POINTER(_Params), C.c_int, C.c_int], S),
         "pbf_adjoint_set_physics": ([_vp, C.c_float, C.c_float], S),
+        "pbf_adjoint_set_spheres": ([_vp, _vp, sz], S),
+        "pbf_adjoint_set_boxes": ([_vp, _vp, sz], S),
+        "pbf_adjoint_set_planes": ([_vp, _vp, sz], S),
         "pbf_adjoint_forward": ([_vp, _vp, _vp, C.c_int, _vp, _vp], S),
         "pbf_adjoint_backward": ([_vp, _vp, _vp, _vp, _vp, C.POINTER(C.c_double),
                                   C.POINTER(C.c_double)], S),
@@ -664,8 +667,8 @@ class PBFAdjoint:
     """Reverse-mode derivative of ``steps`` solver steps (pbf_adjoint_*).
 
     ``forward`` runs the differentiated step (integration, density
-    constraint with s_corr and the container clamp, velocity update, XSPH,
-    vorticity confinement, container velocity response) from (x0, v0),
+    constraint with s_corr and the collision projection, velocity update,
+    XSPH, vorticity confinement, velocity response) from (x0, v0),
     keeping checkpoints;
     ``backward`` takes dL/dx, dL/dv of that forward's final state and returns
     dL/dx0, dL/dv0, dL/drestDensity and dL/dxsphViscosity.  Arrays are (n, 4)
@@ -709,6 +712,19 @@ class PBFAdjoint:
     def set_physics(self, rest_density: float, xsph_viscosity: float):
         self._check(self._L.pbf_adjoint_set_physics(self._h, float(rest_density),
                                                     float(xsph_viscosity)))
+
+    def set_spheres(self, spheres: Iterable):
+        """Sphere colliders of the differentiated step (drops the forward)."""
+        arr = _colliders([_flatten_collider(c) for c in spheres], 4)
+        self._check(self._L.pbf_adjoint_set_spheres(self._h, _ptr(arr), arr.shape[0]))
+
+    def set_boxes(self, boxes: Iterable):
+        arr = _colliders([_flatten_collider(c) for c in boxes], 6)
+        self._check(self._L.pbf_adjoint_set_boxes(self._h, _ptr(arr), arr.shape[0]))
+
+    def set_planes(self, planes: Iterable):
+        arr = _colliders([_flatten_collider(c) for c in planes], 6)
+        self._check(self._L.pbf_adjoint_set_planes(self._h, _ptr(arr), arr.shape[0]))
 
     @staticmethod
     def _arg(a, name, n):

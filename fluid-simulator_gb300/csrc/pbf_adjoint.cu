@@ -2,20 +2,21 @@
 // loss on the final particle state with respect to the initial positions and
 // velocities, the rest density and the XSPH strength.
 //
-// Differentiated substep (container walls only; a step of S substeps is S
-// of them with dt / S, each taped as one step):
+// Differentiated substep (a step of S substeps is S of them with dt / S,
+// each taped as one step):
 //   integrate   v1 = v + g dt, p0 = x + v1 dt               (integration.cu:6-32)
 //   I times     lambda_i = -C_i / (gs^2 (S2_i + |G_i|^2) + eps),
 //               q = p + gs sum_j (lambda_i + lambda_j + s_corr) grad W_ij,
-//               p' = container clamp of q
-//               (pbf_solver_kernels.cu:26-193, collision_kernels.cu:47-82)
+//               p' = collision projection of q (container, spheres, boxes,
+//               planes; pbf_solver_kernels.cu:26-193, collision_kernels.cu:47-234)
 //   velocity    v2 = (p_I - x) / dt                         (pbf_solver_kernels.cu:195-211)
 //   XSPH        v3 = v2 + c sum_j (v2_j - v2_i) W_ij        (pbf_solver_kernels.cu:213-266)
 //   vorticity   v5 = v3 + dt eps (N x w), w_i = sum_j grad W_ij x (v3_j - v3_i),
 //               N = eta / |eta|, eta_i = sum_j (|w_j| - |w_i|) grad W_ij
 //               (pbf_solver_kernels.cu:268-385; only when eps != 0)
-//   response    v4 = wall contacts against v1 (restitution, friction)
-//               (collision_kernels.cu:236-276)
+//   response    v4 = contacts against v1 (restitution, friction; normals of
+//               spheres and boxes depend on the position)
+//               (collision_kernels.cu:236-371)
 // gs = m / rho0, C_i = rho_i / rho0 - 1, rho_i = m (W(0) + sum_j W_ij),
 // G_i = sum_j grad W_ij, S2_i = sum_j |grad W_ij|^2.
 //
@@ -136,79 +137,174 @@ __device__ __forceinline__ float3 lane_sum(float3 v) {
 
 // ---- adjoint -----------------------------------------------------------------
 
-// Container contacts of one particle in the forward's order: up to three
-// walls, each an axis and a normal sign; `active` as resolveContactVelocity
-// decides it for the velocity reaching that wall.
-struct Walls {
-    int m;
-    int axis[3];
-    float sign[3];
-    bool active[3];
+// 3x3 matrices (row-major) for the Jacobians of the collision replays.
+struct Mat3 {
+    float m[9];
 };
-
-__device__ __forceinline__ float comp(float4 v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
-
-__device__ __forceinline__ Walls replay_walls(const StepConst& c, float4 p, float4 vin, float4 v) {
-    Walls w;
-    w.m = 0;
-    const float r = c.particle_radius, eps = kContactEpsilon;
-    const float ts = fsub(1.0f, c.friction);
-    const float minX = fadd(c.col.cminx, r), maxX = fsub(c.col.cmaxx, r);
-    const float minY = fadd(c.col.cminy, r);
-    const float minZ = fadd(c.col.cminz, r), maxZ = fsub(c.col.cmaxz, r);
-    auto wall = [&](int a, float s) {
-        const float nx = a == 0 ? s : 0.0f, ny = a == 1 ? s : 0.0f, nz = a == 2 ? s : 0.0f;
-        const float vn = ffma(v.z, nz, ffma(v.y, ny, fmul(v.x, nx)));
-        const float vinn = ffma(vin.z, nz, ffma(vin.y, ny, fmul(vin.x, nx)));
-        const float target = vinn < 0.0f ? fmul(-c.restitution, vinn) : 0.0f;
-        w.axis[w.m] = a;
-        w.sign[w.m] = s;
-        w.active[w.m] = !(vn > target || (vn == target && vinn >= 0.0f));
-        ++w.m;
-        contact(nx, ny, nz, vin, c.restitution, ts, v);
-    };
-    if (p.x <= fadd(minX, eps)) wall(0, 1.0f);
-    else if (p.x >= fsub(maxX, eps)) wall(0, -1.0f);
-    if (p.y <= fadd(minY, eps)) wall(1, 1.0f);
-    if (p.z <= fadd(minZ, eps)) wall(2, 1.0f);
-    else if (p.z >= fsub(maxZ, eps)) wall(2, -1.0f);
-    return w;
+__device__ __forceinline__ Mat3 mat_diag(float a, float b, float c) {
+    Mat3 r = {{a, 0.0f, 0.0f, 0.0f, b, 0.0f, 0.0f, 0.0f, c}};
+    return r;
+}
+__device__ __forceinline__ Mat3 mat_mul(const Mat3& A, const Mat3& B) {
+    Mat3 r;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+            r.m[3 * i + j] = A.m[3 * i] * B.m[j] + A.m[3 * i + 1] * B.m[3 + j] +
+                             A.m[3 * i + 2] * B.m[6 + j];
+    return r;
+}
+__device__ __forceinline__ Mat3 mat_add(const Mat3& A, const Mat3& B) {
+    Mat3 r;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) r.m[k] = A.m[k] + B.m[k];
+    return r;
+}
+// A^T g.
+__device__ __forceinline__ float3 mat_tmul(const Mat3& A, float3 g) {
+    return make_float3(A.m[0] * g.x + A.m[3] * g.y + A.m[6] * g.z,
+                       A.m[1] * g.x + A.m[4] * g.y + A.m[7] * g.z,
+                       A.m[2] * g.x + A.m[5] * g.y + A.m[8] * g.z);
+}
+// s (I - n n^T).
+__device__ __forceinline__ Mat3 mat_perp(float3 n, float s) {
+    Mat3 r;
+    const float v[3] = {n.x, n.y, n.z};
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) r.m[3 * i + j] = s * ((i == j ? 1.0f : 0.0f) - v[i] * v[j]);
+    return r;
 }
 
-// gv4 -> gv3 (velocity before the contacts, final sorted order) and the
-// gradient of the incoming velocity v1, stored in particle-id order
-// (vin_F[s] = v1[org[s]] in the forward).
+// The projection's Jacobian M = d p / d q over a replay of project_all.
+struct ProjJac {
+    Mat3 M = mat_diag(1.0f, 1.0f, 1.0f);
+    __device__ __forceinline__ void fix(int a) {
+        M.m[3 * a] = M.m[3 * a + 1] = M.m[3 * a + 2] = 0.0f;
+    }
+    __device__ __forceinline__ void sphere(float ox, float oy, float oz, float len, float minD) {
+        const float il = 1.0f / len;
+        M = mat_mul(mat_perp(make_float3(ox * il, oy * il, oz * il), minD * il), M);
+    }
+    // p' = cl + (r / len) o: (I - P) + (r / len) (P - n n^T), P = diag(outside);
+    // n has no component along the inside axes (o_a = 0 there).
+    __device__ __forceinline__ void box(float ox, float oy, float oz, float len, float r,
+                                        bool outx, bool outy, bool outz) {
+        const float il = 1.0f / len;
+        Mat3 J = mat_perp(make_float3(ox * il, oy * il, oz * il), r * il);
+        const bool out[3] = {outx, outy, outz};
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+            if (!out[a]) J.m[4 * a] += 1.0f - r * il;
+        M = mat_mul(J, M);
+    }
+    __device__ __forceinline__ void plane(float nx, float ny, float nz) {
+        M = mat_mul(mat_perp(make_float3(nx, ny, nz), 1.0f), M);
+    }
+    __device__ __forceinline__ void contact(float, float, float, float, bool, bool, bool, float4,
+                                            float4, float, float, float) {}
+};
+
+// The velocity response's Jacobians over a replay of resolve_velocity: with
+// respect to the velocity entering it (A), the incoming velocity v_in (B)
+// and the position (C, through normals that depend on it).  Per active
+// contact with unit normal n:
+//   v' = ts (v - vn n) + target n, vn = v.n, target = -e vin.n when vin.n < 0
+//   dv'/dv = ts (I - n n^T), dv'/dvin = -e n n^T (vin.n < 0),
+//   dv'/dn = -ts (n v^T + vn I) + target I - e n vin^T (vin.n < 0),
+//   dn/dp = (I - n n^T) / len, restricted to the clamped axes for boxes.
+struct RespJac {
+    Mat3 A = mat_diag(1.0f, 1.0f, 1.0f), B = mat_diag(0.0f, 0.0f, 0.0f),
+         C = mat_diag(0.0f, 0.0f, 0.0f);
+    float e = 0.0f, ts = 1.0f;
+    __device__ __forceinline__ void fix(int) {}
+    __device__ __forceinline__ void sphere(float, float, float, float, float) {}
+    __device__ __forceinline__ void box(float, float, float, float, float, bool, bool, bool) {}
+    __device__ __forceinline__ void plane(float, float, float) {}
+    __device__ __forceinline__ void contact(float nx, float ny, float nz, float len, bool outx,
+                                            bool outy, bool outz, float4 vin, float4 v,
+                                            float vn, float vinn, float target) {
+        const float3 n = make_float3(nx, ny, nz);
+        const Mat3 Fv = mat_perp(n, ts);
+        A = mat_mul(Fv, A);
+        B = mat_mul(Fv, B);
+        C = mat_mul(Fv, C);
+        const float nv[3] = {nx, ny, nz};
+        const bool hit = vinn < 0.0f;
+        if (hit) {
+            Mat3 Fvin;
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) Fvin.m[3 * i + j] = -e * nv[i] * nv[j];
+            B = mat_add(B, Fvin);
+        }
+        if (len > 0.0f) {
+            const float vv[3] = {v.x, v.y, v.z}, vi[3] = {vin.x, vin.y, vin.z};
+            Mat3 Fn;
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j)
+                    Fn.m[3 * i + j] = -ts * nv[i] * vv[j] + (i == j ? target - ts * vn : 0.0f) -
+                                      (hit ? e * nv[i] * vi[j] : 0.0f);
+            Mat3 Np = mat_perp(n, 1.0f / len);
+            const bool out[3] = {outx, outy, outz};
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                if (!out[j]) Np.m[j] = Np.m[3 + j] = Np.m[6 + j] = 0.0f;
+            C = mat_add(C, mat_mul(Fn, Np));
+        }
+    }
+};
+
+// gv' (velocity leaving the contacts, particle-id order through org) ->
+// gradient of the velocity entering the contacts (final sorted order), of
+// the incoming velocity v1 (particle-id order; vin_F[s] = v1[org[s]] in the
+// forward) and of the position (gxe, final sorted order: the contact normals
+// of spheres and boxes depend on it).
 __global__ void k_respond_adj(const float4* __restrict__ pF, const float4* __restrict__ vinF,
-                              const float4* __restrict__ v3, const float4* __restrict__ gv4,
+                              const float4* __restrict__ vc, const float4* __restrict__ gv4,
                               const uint32_t* __restrict__ org, StepConst c, int n,
-                              float4* __restrict__ gv3, float4* __restrict__ gv1) {
+                              float4* __restrict__ gv3, float4* __restrict__ gv1,
+                              float4* __restrict__ gxe) {
     const int s = blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= n) return;
     const uint32_t o = org[s];
     if (o >= static_cast<uint32_t>(n)) return;  // only after a failed forward
-    const float4 vin = vinF[s];
-    const Walls w = replay_walls(c, pF[s], vin, v3[s]);
-    const float4 g4 = gv4[o];
-    float g[3] = {g4.x, g4.y, g4.z};
-    float gin[3] = {0.0f, 0.0f, 0.0f};
-    const float ts = 1.0f - c.friction;
-    for (int k = w.m - 1; k >= 0; --k) {
-        if (!w.active[k]) continue;
-        const int a = w.axis[k];
-        // v'_a = -e vin_a when the incoming normal speed is negative, else 0;
-        // v'_b = (1 - friction) v_b for the other axes.
-        if (w.sign[k] * comp(vin, a) < 0.0f) gin[a] += -c.restitution * g[a];
-        g[a] = 0.0f;
-        for (int b = 0; b < 3; ++b)
-            if (b != a) g[b] *= ts;
-    }
-    gv3[s] = make_float4(g[0], g[1], g[2], 0.0f);
-    gv1[o] = make_float4(gin[0], gin[1], gin[2], 0.0f);
+    RespJac jac;
+    jac.e = c.restitution;
+    jac.ts = fsub(1.0f, c.friction);
+    float4 v = vc[s];
+    resolve_velocity(c.col, c.particle_radius, c.restitution, c.friction, pF[s], vinF[s], v, jac);
+    const float3 g = f3(gv4[o]);
+    const float3 a = mat_tmul(jac.A, g), b = mat_tmul(jac.B, g), x = mat_tmul(jac.C, g);
+    gv3[s] = make_float4(a.x, a.y, a.z, 0.0f);
+    gv1[o] = make_float4(b.x, b.y, b.z, 0.0f);
+    gxe[s] = make_float4(x.x, x.y, x.z, 0.0f);
 }
 
 // The gradient of q where the projection moved no component, 0 elsewhere.
 __device__ __forceinline__ float4 unmoved(uint8_t m, float3 g) {
     return make_float4((m & 1u) ? 0.0f : g.x, (m & 2u) ? 0.0f : g.y, (m & 4u) ? 0.0f : g.z, 0.0f);
+}
+
+// Gradient of the position before the collision projection at slot r: with
+// sphere / box / plane colliders the transpose of the projection's Jacobian,
+// replayed from the recorded position before it (pre); with the container
+// alone the moved bits say which components were clamped.
+__device__ __forceinline__ float4 project_adj(const StepConst& c, const float4* __restrict__ pre,
+                                              const uint8_t* __restrict__ moved, uint32_t r,
+                                              float3 g) {
+    if (!pre) return unmoved(moved[r], g);
+    const float4 q = pre[r];
+    float px = q.x, py = q.y, pz = q.z;
+    ProjJac jac;
+    project_all(c.col, c.particle_radius, px, py, pz, jac);
+    const float3 t = mat_tmul(jac.M, g);
+    return make_float4(t.x, t.y, t.z, 0.0f);
 }
 
 // XSPH and velocity-update adjoint in the final sorted order, then the final
@@ -219,14 +315,16 @@ __device__ __forceinline__ float4 unmoved(uint8_t m, float3 g) {
 //   dL/dc += gv3_i . sum_j (v2_j - v2_i) W_ij
 //   gq_{I-1} at slot rel[s] of the last iteration's order = gp_F where the
 //   projection left the component unchanged, 0 elsewhere.
-// gx_vort (optional): position gradient from the vorticity confinement.
+// gx_extra: position gradient from the contact normals and the vorticity
+// confinement.
 template <int L>
 __global__ void k_xsph_adj(const float4* __restrict__ pF, const float4* __restrict__ v2,
                            const float4* __restrict__ gv3, const uint32_t* __restrict__ nbr,
                            const int* __restrict__ cnt, const float4* __restrict__ gx_next,
                            const uint32_t* __restrict__ org, const uint32_t* __restrict__ rel,
                            const uint8_t* __restrict__ moved_last,
-                           const float4* __restrict__ gx_vort, StepConst c, int n,
+                           const float4* __restrict__ pre_last,
+                           const float4* __restrict__ gx_extra, StepConst c, int n,
                            float4* __restrict__ gxs, float4* __restrict__ gq,
                            double* __restrict__ acc_c) {
     const int tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -255,9 +353,9 @@ __global__ void k_xsph_adj(const float4* __restrict__ pF, const float4* __restri
     const uint32_t o = org[i], r = rel[i];
     if (o >= static_cast<uint32_t>(n) || r >= static_cast<uint32_t>(n)) return;
     float3 gp = f3(gx_next[o]) + c.inv_dt * gv2 + c.xsph_c * pos;
-    if (gx_vort) gp = gp + f3(gx_vort[i]);  // vorticity confinement's position terms
+    gp = gp + f3(gx_extra[i]);  // contact normals' and vorticity confinement's terms
     gxs[o] = make_float4(-c.inv_dt * gv2.x, -c.inv_dt * gv2.y, -c.inv_dt * gv2.z, 0.0f);
-    gq[r] = unmoved(moved_last[r], gp);
+    gq[r] = project_adj(c, pre_last, moved_last, r, gp);
 }
 
 // First gather pass of one iteration's adjoint (u_ij = gq_i - gq_j):
@@ -332,6 +430,7 @@ __global__ void k_iter_adj_b(const float4* __restrict__ p, const float4* __restr
                              const int* __restrict__ cnt, const float4* __restrict__ gpart,
                              const uint32_t* __restrict__ rel,
                              const uint8_t* __restrict__ moved_prev,
+                             const float4* __restrict__ pre_prev,
                              const float4* __restrict__ gxs, const float4* __restrict__ gv1,
                              StepConst c, int n, float4* __restrict__ gq_prev,
                              float4* __restrict__ gx_t, float4* __restrict__ gv_t) {
@@ -360,7 +459,7 @@ __global__ void k_iter_adj_b(const float4* __restrict__ p, const float4* __restr
     const uint32_t r = rel[i];
     if (r >= static_cast<uint32_t>(n)) return;  // only after a failed forward
     if (moved_prev) {
-        gq_prev[r] = unmoved(moved_prev[r], gp);
+        gq_prev[r] = project_adj(c, pre_prev, moved_prev, r, gp);
     } else {
         // p0 = x + v1 dt, v1 = v + g dt.
         const float4 gs = gxs[r], g1 = gv1[r];
@@ -414,7 +513,7 @@ __global__ void k_conf_adj_a(const float4* __restrict__ pF, const float4* __rest
 // Second pass: the magnitude terms of eta,
 //   gm_k = -sum_j (geta_k + geta_j) . g_kj,
 //   gx_k = sum_j (m_j - m_k) H_kj (geta_k + geta_j),
-// and gw_k = direct + gm_k w_k / m_k.
+// (added to gx) and gw_k = direct + gm_k w_k / m_k.
 template <int L>
 __global__ void k_conf_adj_b(const float4* __restrict__ pF, const float4* __restrict__ om,
                              const uint32_t* __restrict__ nbr, const int* __restrict__ cnt,
@@ -444,7 +543,8 @@ __global__ void k_conf_adj_b(const float4* __restrict__ pF, const float4* __rest
     float3 g = f3(gw_direct[i]);
     if (mi > 0.0f) g = g + (gm / mi) * f3(om[i]);
     gw[i] = make_float4(g.x, g.y, g.z, 0.0f);
-    gx[i] = make_float4(pos.x, pos.y, pos.z, 0.0f);
+    const float4 x0 = gx[i];
+    gx[i] = make_float4(x0.x + pos.x, x0.y + pos.y, x0.z + pos.z, 0.0f);
 }
 
 // Third pass: the vorticity sum,
@@ -542,10 +642,16 @@ struct pbf_adjoint {
     // The tape holds the last segment of the latest forward (recorded by the
     // forward itself, so the backward need not recompute it).
     bool tape_last = false;
-    // Adjoint work arrays (gva..gvx: vorticity confinement only).
-    DeviceBuffer gx, gv, gxs, gv1, gv3, gq0, gq1, gpart, aux, aa, acc_r, acc_c;
-    DeviceBuffer gva, gvb, gvc, gvx;
+    // Adjoint work arrays (gva..gvc: vorticity confinement only; gxe: the
+    // position gradient from contact normals and vorticity confinement).
+    DeviceBuffer gx, gv, gxs, gv1, gv3, gq0, gq1, gpart, aux, aa, acc_r, acc_c, gxe;
+    DeviceBuffer gva, gvb, gvc;
     bool vort = false;  // vorticity confinement in the step
+    // Sphere, box and plane colliders (host records as the solver keeps them,
+    // and their device copy).
+    std::vector<float4> h_col[3];
+    DeviceBuffer d_col;
+    bool has_col() const { return !h_col[0].empty() || !h_col[1].empty() || !h_col[2].empty(); }
     // Captured segments: (kind, length, parity) -> graph.
     std::map<std::tuple<int, int, int>, cudaGraphExec_t> graphs;
 
@@ -568,7 +674,7 @@ struct pbf_adjoint {
     // permutation of sort k (its slot s takes slot REL[s] of the previous
     // order; for k = 0 that order is particle-id order), and ORG(t) the
     // composed permutation of the final order (slot -> particle id).
-    int f4_per_step() const { return iters + (vort ? 6 : 4); }
+    int f4_per_step() const { return iters + (vort ? 6 : 4) + iters; }
     int u32_per_step() const { return iters + 2; }
     float4* P(int t, int k) {
         return tf4.as<float4>() + (static_cast<size_t>(t) * f4_per_step() + k) * n;
@@ -580,6 +686,9 @@ struct pbf_adjoint {
     float4* V5(int t) { return P(t, iters + 5); }
     // Velocities entering the contact response.
     float4* VC(int t) { return vort ? V5(t) : V3(t); }
+    // Positions of iteration k before the collision projection (written only
+    // with sphere / box / plane colliders).
+    float4* PRE(int t, int k) { return P(t, iters + (vort ? 6 : 4) + k); }
     uint32_t* REL(int t, int k) {
         return tu32.as<uint32_t>() + (static_cast<size_t>(t) * u32_per_step() + k) * n;
     }
@@ -658,6 +767,7 @@ struct pbf_adjoint {
         c.col.cmaxx = hi.x;
         c.col.cmaxy = hi.y;
         c.col.cmaxz = hi.z;
+        apply_colliders();
 
         const size_t f4b = n * sizeof(float4), u4b = n * sizeof(uint32_t);
         const size_t E = static_cast<size_t>(every), I = static_cast<size_t>(iters);
@@ -678,9 +788,9 @@ struct pbf_adjoint {
         tnb.allocate(E * (I + 1) * stride * max_nb * sizeof(uint32_t));
         tcn.allocate(E * (I + 1) * u4b);
         states.allocate((E + 1) * 2 * f4b);
-        for (DeviceBuffer* b : {&gx, &gv, &gxs, &gv1, &gv3, &gq0, &gq1, &gpart, &aux})
+        for (DeviceBuffer* b : {&gx, &gv, &gxs, &gv1, &gv3, &gq0, &gq1, &gpart, &aux, &gxe})
             b->allocate(f4b);
-        for (DeviceBuffer* b : {&gva, &gvb, &gvc, &gvx}) {
+        for (DeviceBuffer* b : {&gva, &gvb, &gvc}) {
             if (vort)
                 b->allocate(f4b);
             else
@@ -697,6 +807,40 @@ struct pbf_adjoint {
         ckpt = DeviceBuffer();
         tape_last = false;
         steps_done = 0;
+    }
+
+    // CollisionSystem setters for the differentiated step (kind 0 spheres, 1
+    // boxes, 2 planes; validated as the solver's); drops the recorded
+    // forward.  Kept across initialize.
+    void set_colliders(int kind, const void* data, size_t count) {
+        std::vector<float4> next = collider_records(kind, data, count);
+        cuda_check(cudaSetDevice(device));
+        std::vector<float4> all;
+        for (int k = 0; k < 3; ++k) {
+            const std::vector<float4>& v = k == kind ? next : h_col[k];
+            all.insert(all.end(), v.begin(), v.end());
+        }
+        DeviceBuffer d(all.size() * sizeof(float4));
+        if (!all.empty())
+            cuda_check(cudaMemcpy(d.get(), all.data(), all.size() * sizeof(float4),
+                                  cudaMemcpyHostToDevice));
+        h_col[kind].swap(next);
+        d_col = std::move(d);
+        apply_colliders();
+        clear_graphs();  // the graphs hold the old constants
+        ckpt = DeviceBuffer();
+        tape_last = false;
+        steps_done = 0;
+    }
+    void apply_colliders() {
+        const float4* base = d_col.as<float4>();
+        const size_t ns = h_col[0].size(), nb = h_col[1].size() / 2, np = h_col[2].size() / 2;
+        c.col.spheres = base;
+        c.col.boxes = base ? base + ns : nullptr;
+        c.col.planes = base ? base + ns + 2 * nb : nullptr;
+        c.col.ns = static_cast<int>(ns);
+        c.col.nb = static_cast<int>(nb);
+        c.col.np = static_cast<int>(np);
     }
 
     // New rest density and XSPH strength (validated like initialize).
@@ -750,7 +894,8 @@ struct pbf_adjoint {
             launch_search(P(t, k), s0, s0 + soa_stride(), s0 + 2 * soa_stride(), first.as<int>(), c,
                           N, NB(t, k), CN(t, k), LAM(t, k), sp, true, stream);
             launch_delta_apply(P(t, k), NB(t, k), CN(t, k), LAM(t, k), c, N, pn.as<float4>(),
-                               keys.as<uint32_t>(), sp, stream, MV(t, k));
+                               keys.as<uint32_t>(), sp, stream, MV(t, k),
+                               has_col() ? PRE(t, k) : nullptr);
             src = pn.as<float4>();
             org_in = org_out;
         }
@@ -785,40 +930,42 @@ struct pbf_adjoint {
         const int I = iters;
         const unsigned gl = adj::grid_lanes(N, L);
         float4* pF = P(t, I);
+        // gv3: gradient of the velocities entering the contacts; gxe: the
+        // position terms of contact normals (then of vorticity confinement).
         adj::k_respond_adj<<<adj::grid(N), adj::kB, 0, stream>>>(
             pF, VINF(t), VC(t), gv.as<float4>(), ORG(t), c, N, gv3.as<float4>(),
-            gv1.as<float4>());
-        // gv3 holds the gradient of the velocities entering the contacts; with
-        // vorticity confinement its three passes turn that into the gradient
-        // of the XSPH output (gvb) plus position terms (gvx).
+            gv1.as<float4>(), gxe.as<float4>());
+        // With vorticity confinement its three passes turn gv3 into the
+        // gradient of the XSPH output (gvb).
         const float4* g_xsph_out = gv3.as<float4>();
-        const float4* gx_vort = nullptr;
         if (vort) {
             adj::k_conf_adj_a<L><<<gl, adj::kB, 0, stream>>>(
                 pF, OM(t), NB(t, I), CN(t, I), gv3.as<float4>(), c, N, gva.as<float4>(),
                 gvb.as<float4>());
             adj::k_conf_adj_b<L><<<gl, adj::kB, 0, stream>>>(
                 pF, OM(t), NB(t, I), CN(t, I), gva.as<float4>(), gvb.as<float4>(), c, N,
-                gvc.as<float4>(), gvx.as<float4>());
+                gvc.as<float4>(), gxe.as<float4>());
             adj::k_vort_adj<L><<<gl, adj::kB, 0, stream>>>(
                 pF, V3(t), NB(t, I), CN(t, I), gvc.as<float4>(), gv3.as<float4>(), c, N,
-                gvb.as<float4>(), gvx.as<float4>());
+                gvb.as<float4>(), gxe.as<float4>());
             g_xsph_out = gvb.as<float4>();
-            gx_vort = gvx.as<float4>();
         }
+        const bool col = has_col();
         float4* gqa = gq0.as<float4>();
         float4* gqb = gq1.as<float4>();
         adj::k_xsph_adj<L><<<gl, adj::kB, 0, stream>>>(
             pF, V2(t), g_xsph_out, NB(t, I), CN(t, I), gx.as<float4>(), ORG(t), REL(t, I),
-            MV(t, I - 1), gx_vort, c, N, gxs.as<float4>(), gqa, acc_c.as<double>());
+            MV(t, I - 1), col ? PRE(t, I - 1) : nullptr, gxe.as<float4>(), c, N,
+            gxs.as<float4>(), gqa, acc_c.as<double>());
         for (int k = I - 1; k >= 0; --k) {
             adj::k_iter_adj_a<L><<<gl, adj::kB, 0, stream>>>(
                 P(t, k), LAM(t, k), gqa, NB(t, k), CN(t, k), c, N, gpart.as<float4>(),
                 aux.as<float4>(), aa.as<float>(), acc_r.as<double>());
             adj::k_iter_adj_b<L><<<gl, adj::kB, 0, stream>>>(
                 P(t, k), aux.as<float4>(), aa.as<float>(), NB(t, k), CN(t, k),
-                gpart.as<float4>(), REL(t, k), k > 0 ? MV(t, k - 1) : nullptr, gxs.as<float4>(),
-                gv1.as<float4>(), c, N, gqb, gx.as<float4>(), gv.as<float4>());
+                gpart.as<float4>(), REL(t, k), k > 0 ? MV(t, k - 1) : nullptr,
+                (k > 0 && col) ? PRE(t, k - 1) : nullptr, gxs.as<float4>(), gv1.as<float4>(), c,
+                N, gqb, gx.as<float4>(), gv.as<float4>());
             std::swap(gqa, gqb);
         }
         cuda_check(cudaGetLastError());
@@ -1001,6 +1148,18 @@ pbf_status pbf_adjoint_initialize(pbf_adjoint* a, size_t count, pbf_float3 min_b
 
 pbf_status pbf_adjoint_set_physics(pbf_adjoint* a, float rest_density, float xsph_viscosity) {
     PBF_ADJ_GUARD(a, a->set_physics(rest_density, xsph_viscosity));
+}
+
+pbf_status pbf_adjoint_set_spheres(pbf_adjoint* a, const pbf_sphere* spheres, size_t count) {
+    PBF_ADJ_GUARD(a, a->set_colliders(0, spheres, count));
+}
+
+pbf_status pbf_adjoint_set_boxes(pbf_adjoint* a, const pbf_box* boxes, size_t count) {
+    PBF_ADJ_GUARD(a, a->set_colliders(1, boxes, count));
+}
+
+pbf_status pbf_adjoint_set_planes(pbf_adjoint* a, const pbf_plane* planes, size_t count) {
+    PBF_ADJ_GUARD(a, a->set_colliders(2, planes, count));
 }
 
 pbf_status pbf_adjoint_forward(pbf_adjoint* a, const pbf_float4* x0, const pbf_float4* v0,

@@ -9,6 +9,7 @@
 #include <stdexcept>
 #include <string>
 #include <utility>
+#include <vector>
 
 #include "pbf103.h"
 
@@ -29,6 +30,10 @@ struct Failure : std::runtime_error {
 bool finite3(pbf_float3 v);
 void validate_params(const pbf_params& p);
 std::array<int, 3> grid_dims_checked(pbf_float3 mn, pbf_float3 mx, float cell);
+// Validated device records of colliders (CollisionSystem setters,
+// src/pbf/collision_system.cu:53-126): kind 0 spheres (center, radius), 1
+// boxes (center, -), (halfExtents, -), 2 planes (point, -), (normal, -).
+std::vector<float4> collider_records(int kind, const void* data, size_t count);
 
 inline void cuda_check(cudaError_t e) {
     if (e != cudaSuccess) fail(PBF_ERR_RUNTIME, cudaGetErrorString(e));

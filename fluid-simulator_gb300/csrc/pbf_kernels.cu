@@ -638,12 +638,14 @@ __device__ __forceinline__ void delta_sum(const StepConst& c, const float4* __re
 // delta p + applyDeltaPosition + CollisionSystem::solve + next cell keys.
 // N: artificial-pressure exponent fixed at compile time (0 = read at run time).
 // moved (optional): bit a set where the projection changed component a.
+// pre (optional): the position before the projection.
 template <int N, bool B>
 __global__ void PBF_GATHER_REGS(48)
 k_delta_apply(const float4* __restrict__ xs, const uint32_t* __restrict__ nbr,
               const int* __restrict__ cnt, const float* __restrict__ lam, StepConst c, int n,
               float4* __restrict__ xs_out, uint32_t* __restrict__ keys_out,
-              uint8_t* __restrict__ moved, unsigned* __restrict__ status) {
+              uint8_t* __restrict__ moved, float4* __restrict__ pre,
+              unsigned* __restrict__ status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || fatal(status)) return;
     const float4 pi = xs[i];
@@ -657,6 +659,7 @@ k_delta_apply(const float4* __restrict__ xs, const uint32_t* __restrict__ nbr,
     }
     float px = fadd(pi.x, dpx), py = fadd(pi.y, dpy), pz = fadd(pi.z, dpz);
     const float ux = px, uy = py, uz = pz;
+    if (pre) pre[i] = make_float4(ux, uy, uz, pi.w);
     if (!project_all(colliders_of<B>(c, i), c.particle_radius, px, py, pz))
         atomicOr(status, kStatusNotConverged);
     if (moved)
@@ -1104,12 +1107,12 @@ void launch_nb_scan(const int* cnt, uint32_t* off, size_t cap, int n, uint32_t* 
 template <bool B>
 void launch_delta_apply_b(const float4* xs, const uint32_t* nbr, const int* cnt, const float* lam,
                           const StepConst& c, int n, float4* xs_out, uint32_t* keys_out,
-                          uint8_t* moved, unsigned* status, cudaStream_t st) {
+                          uint8_t* moved, float4* pre, unsigned* status, cudaStream_t st) {
     const int bs = tuned_block(c, kTunedDelta);
     const unsigned g = blocks_for(n, bs);
 #define PBF_DELTA_CASE(N)                                                                        \
     launch_k(k_delta_apply<N, B>, g, bs, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out, moved,   \
-             status)
+             pre, status)
     switch (c.sc.k != 0.0f ? c.sc.n : 0) {
         case 1: PBF_DELTA_CASE(1); break;
         case 2: PBF_DELTA_CASE(2); break;
@@ -1121,11 +1124,13 @@ void launch_delta_apply_b(const float4* xs, const uint32_t* nbr, const int* cnt,
 }
 void launch_delta_apply(const float4* xs, const uint32_t* nbr, const int* cnt, const float* lam,
                         const StepConst& c, int n, float4* xs_out, uint32_t* keys_out,
-                        unsigned* status, cudaStream_t st, uint8_t* moved) {
+                        unsigned* status, cudaStream_t st, uint8_t* moved, float4* pre) {
     if (c.scenes)
-        launch_delta_apply_b<true>(xs, nbr, cnt, lam, c, n, xs_out, keys_out, moved, status, st);
+        launch_delta_apply_b<true>(xs, nbr, cnt, lam, c, n, xs_out, keys_out, moved, pre, status,
+                                   st);
     else
-        launch_delta_apply_b<false>(xs, nbr, cnt, lam, c, n, xs_out, keys_out, moved, status, st);
+        launch_delta_apply_b<false>(xs, nbr, cnt, lam, c, n, xs_out, keys_out, moved, pre, status,
+                                    st);
 }
 void launch_finalize(const uint32_t* org, const float4* x_old, const float4* vin_old,
                      const float4* v_old, const uint32_t* id_old, const float4* xs, int n,

@@ -98,10 +98,12 @@ void launch_search_xsph(const float4* xs, const float* sx, const float* sy, cons
                         const float4* v, float4* v_out, const float4* vin, bool resolve,
                         unsigned* status, cudaStream_t st);
 // moved (optional): per slot, bit a set where the collision projection
-// changed component a of the position.
+// changed component a of the position; pre (optional): the position before
+// the projection.
 void launch_delta_apply(const float4* xs, const uint32_t* nbr, const int* cnt, const float* lam,
                         const StepConst& c, int n, float4* xs_out, uint32_t* keys_out,
-                        unsigned* status, cudaStream_t st, uint8_t* moved = nullptr);
+                        unsigned* status, cudaStream_t st, uint8_t* moved = nullptr,
+                        float4* pre = nullptr);
 // Compact lists: neighbour counts of the walk (no list written), then the
 // exclusive scan of the counts into off (n + 1 entries; a total above cap
 // sets kStatusListOverflow).  scratch: nb_scan_scratch_words(n) words.

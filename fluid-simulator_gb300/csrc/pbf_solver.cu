@@ -91,6 +91,42 @@ namespace pbf {
 bool finite3(pbf_float3 v) { return std::isfinite(v.x) && std::isfinite(v.y) && std::isfinite(v.z); }
 
 // Parameter validation of PBFSolver::initialize (src/pbf/pbf_solver.cu:45-79).
+std::vector<float4> collider_records(int kind, const void* data, size_t count) {
+    std::vector<float4> next;
+    if (kind == 0) {
+        const pbf_sphere* s = static_cast<const pbf_sphere*>(data);
+        if (count && !s) fail(PBF_ERR_INVALID_ARGUMENT, "Sphere array must not be null");
+        for (size_t i = 0; i < count; ++i) {
+            if (!finite3(s[i].center) || !std::isfinite(s[i].radius) || s[i].radius <= 0.0f)
+                fail(PBF_ERR_INVALID_ARGUMENT, "Sphere radius must be positive");
+            next.push_back(make_float4(s[i].center.x, s[i].center.y, s[i].center.z, s[i].radius));
+        }
+    } else if (kind == 1) {
+        const pbf_box* b = static_cast<const pbf_box*>(data);
+        if (count && !b) fail(PBF_ERR_INVALID_ARGUMENT, "Box array must not be null");
+        for (size_t i = 0; i < count; ++i) {
+            const pbf_float3 c = b[i].center, e = b[i].halfExtents;
+            if (!finite3(c) || !std::isfinite(e.x) || e.x <= 0.0f || !std::isfinite(e.y) ||
+                e.y <= 0.0f || !std::isfinite(e.z) || e.z <= 0.0f)
+                fail(PBF_ERR_INVALID_ARGUMENT, "Box half extents must be positive");
+            next.push_back(make_float4(c.x, c.y, c.z, 0.0f));
+            next.push_back(make_float4(e.x, e.y, e.z, 0.0f));
+        }
+    } else {
+        const pbf_plane* p = static_cast<const pbf_plane*>(data);
+        if (count && !p) fail(PBF_ERR_INVALID_ARGUMENT, "Plane array must not be null");
+        for (size_t i = 0; i < count; ++i) {
+            const pbf_float3 q = p[i].point, nn = p[i].normal;
+            const float l2 = nn.x * nn.x + nn.y * nn.y + nn.z * nn.z;
+            if (!finite3(q) || !std::isfinite(l2) || l2 == 0.0f)
+                fail(PBF_ERR_INVALID_ARGUMENT, "Plane normal must not be zero");
+            next.push_back(make_float4(q.x, q.y, q.z, 0.0f));
+            next.push_back(make_float4(nn.x, nn.y, nn.z, 0.0f));
+        }
+    }
+    return next;
+}
+
 void validate_params(const pbf_params& p) {
     if (!std::isfinite(p.dt) || p.dt <= 0.0f || !std::isfinite(p.restDensity) ||
         p.restDensity <= 0.0f || !std::isfinite(p.particleMass) || p.particleMass <= 0.0f ||
@@ -818,41 +854,8 @@ struct pbf_solver {
     }
 
     void set_colliders(int kind, const void* data, size_t count) {
-        std::vector<float4> next;
-        if (kind == 0) {
-            const pbf_sphere* s = static_cast<const pbf_sphere*>(data);
-            if (count && !s) fail(PBF_ERR_INVALID_ARGUMENT, "Sphere array must not be null");
-            for (size_t i = 0; i < count; ++i) {
-                if (!finite3(s[i].center) || !std::isfinite(s[i].radius) || s[i].radius <= 0.0f)
-                    fail(PBF_ERR_INVALID_ARGUMENT, "Sphere radius must be positive");
-                next.push_back(make_float4(s[i].center.x, s[i].center.y, s[i].center.z, s[i].radius));
-            }
-            h_spheres.swap(next);
-        } else if (kind == 1) {
-            const pbf_box* b = static_cast<const pbf_box*>(data);
-            if (count && !b) fail(PBF_ERR_INVALID_ARGUMENT, "Box array must not be null");
-            for (size_t i = 0; i < count; ++i) {
-                const pbf_float3 c = b[i].center, e = b[i].halfExtents;
-                if (!finite3(c) || !std::isfinite(e.x) || e.x <= 0.0f || !std::isfinite(e.y) ||
-                    e.y <= 0.0f || !std::isfinite(e.z) || e.z <= 0.0f)
-                    fail(PBF_ERR_INVALID_ARGUMENT, "Box half extents must be positive");
-                next.push_back(make_float4(c.x, c.y, c.z, 0.0f));
-                next.push_back(make_float4(e.x, e.y, e.z, 0.0f));
-            }
-            h_boxes.swap(next);
-        } else {
-            const pbf_plane* p = static_cast<const pbf_plane*>(data);
-            if (count && !p) fail(PBF_ERR_INVALID_ARGUMENT, "Plane array must not be null");
-            for (size_t i = 0; i < count; ++i) {
-                const pbf_float3 q = p[i].point, nn = p[i].normal;
-                const float l2 = nn.x * nn.x + nn.y * nn.y + nn.z * nn.z;
-                if (!finite3(q) || !std::isfinite(l2) || l2 == 0.0f)
-                    fail(PBF_ERR_INVALID_ARGUMENT, "Plane normal must not be zero");
-                next.push_back(make_float4(q.x, q.y, q.z, 0.0f));
-                next.push_back(make_float4(nn.x, nn.y, nn.z, 0.0f));
-            }
-            h_planes.swap(next);
-        }
+        std::vector<float4> next = collider_records(kind, data, count);
+        (kind == 0 ? h_spheres : kind == 1 ? h_boxes : h_planes).swap(next);
         colliders_dirty = true;
         clear_graphs();
     }

@@ -169,15 +169,17 @@ pbf_status pbf_block_sizes(const pbf_solver* s, int* sizes, int count);
  * Gradients of a loss on the final state of `steps` steps with respect to
  * the initial positions and velocities, restDensity (mass held fixed) and
  * xsphViscosity.  The differentiated step is integration, the density
- * constraint iterations with s_corr and the container clamp, the velocity
- * update, XSPH, vorticity confinement and the container velocity response,
+ * constraint iterations with s_corr and the collision projection, the velocity
+ * update, XSPH, vorticity confinement and the velocity response,
  * over neighbour lists
  * recorded by the forward (integer data, not differentiated).  The forward
  * runs the solver's own kernels: with one substep, one step from a state in
  * particle-id order is bit for bit pbf_step on that state; every substep
  * returns to particle-id order, so forward(x, v, a + b) equals
  * forward(forward(x, v, a), b).  A step of S substeps is taped as S substeps
- * of dt / S (checkpoint_every counts steps).  No sphere/box/plane colliders.  The forward keeps (x, v) every `checkpoint_every` steps and
+ * of dt / S (checkpoint_every counts steps).  Sphere, box and plane colliders
+ * (pbf_adjoint_set_*) are differentiated through replays of the projection
+ * and the contact response.  The forward keeps (x, v) every `checkpoint_every` steps and
  * records its last segment; the backward recomputes each earlier segment
  * from its checkpoint.  State and gradient pointers may be host or device
  * memory.  Gradient arrays are float4 with w ignored. */
@@ -190,6 +192,11 @@ pbf_status pbf_adjoint_initialize(pbf_adjoint* a, size_t count, pbf_float3 min_b
                                   int max_neighbors, int checkpoint_every);
 /* Replace restDensity and xsphViscosity (drops the recorded forward). */
 pbf_status pbf_adjoint_set_physics(pbf_adjoint* a, float rest_density, float xsph_viscosity);
+/* Colliders of the differentiated step, validated like pbf_set_spheres /
+ * _boxes / _planes (count 0 clears; drops the recorded forward). */
+pbf_status pbf_adjoint_set_spheres(pbf_adjoint* a, const pbf_sphere* spheres, size_t count);
+pbf_status pbf_adjoint_set_boxes(pbf_adjoint* a, const pbf_box* boxes, size_t count);
+pbf_status pbf_adjoint_set_planes(pbf_adjoint* a, const pbf_plane* planes, size_t count);
 pbf_status pbf_adjoint_forward(pbf_adjoint* a, const pbf_float4* x0, const pbf_float4* v0,
                                int steps, pbf_float4* x_out, pbf_float4* v_out);
 /* grad_x / grad_v: dL/dx, dL/dv of the last forward's final state;

@@ -103,6 +103,17 @@ def test_invalid_compact_list_capacity(pbf):
         s.initialize(8, (0, 0, 0), (1, 1, 1), SP(**P(dt=0.0)), list_capacity=64)
 
 
+def test_adjoint_collider_validation(pbf):
+    a = pbf.PBFAdjoint()
+    with pytest.raises(pbf.InvalidArgument):
+        a.set_spheres([((0.0, 0.0, 0.0), 0.0)])
+    with pytest.raises(pbf.InvalidArgument):
+        a.set_boxes([((0.0, 0.0, 0.0), (1.0, -1.0, 1.0))])
+    with pytest.raises(pbf.InvalidArgument):
+        a.set_planes([((0.0, 0.0, 0.0), (0.0, 0.0, 0.0))])
+    a.close()
+
+
 INVALID = [
     dict(dt=0.0), dict(dt=math.nan), dict(dt=1.4e-45, substeps=2),
     dict(restDensity=-1.0), dict(restDensity=math.inf),

@@ -239,3 +239,101 @@ def test_adjoint_matches_fp64_tangents_along_its_trajectory(pbf, scenes, orc, vo
     adj = np.array([(g * dirs[0]).sum(), (g * dirs[1]).sum(), (g * dirs[2]).sum(), gr, gc])
     rel = np.abs(adj - jvp) / np.abs(jvp)
     assert (rel <= 1e-3).all(), (adj, jvp, rel)
+
+
+# Colliders grazing the 16x16x8 lattice (x, y in [0.025, 0.8], z in
+# [0.025, 0.4]): a sphere and a box reaching into its top layers and a
+# slightly tilted floor a few millimetres into its bottom layer, so most
+# particles feel a projection or a contact while the step stays well
+# conditioned (colliders deep in the fluid push particles out violently and
+# make the derivatives grow by orders of magnitude).
+_N = np.array([0.02, 1.0, 0.0]) / np.linalg.norm([0.02, 1.0, 0.0])
+COLLIDERS = dict(spheres=[(0.2, 0.9, 0.2, 0.12)], boxes=[(0.6, 0.85, 0.2, 0.05, 0.06, 0.05)],
+                 planes=[(0.4, 0.0, 0.2) + tuple(float(v) for v in _N)])
+
+
+def with_colliders(obj):
+    obj.set_spheres(COLLIDERS["spheres"])
+    obj.set_boxes(COLLIDERS["boxes"])
+    obj.set_planes(COLLIDERS["planes"])
+    return obj
+
+
+def check_gradient(adj, jvp, ndirs, tol=1e-3):
+    """Random v0 directions: the whole-gradient relative error estimated
+    from the projections (for Gaussian r, E[(e.r)^2] = |e|^2; a single random
+    projection may nearly cancel).  Parameters: each relative error."""
+    e = adj[:ndirs] - jvp[:ndirs]
+    grad = np.sqrt((e ** 2).sum() / (jvp[:ndirs] ** 2).sum())
+    par = np.abs(adj[ndirs:] - jvp[ndirs:]) / np.abs(jvp[ndirs:])
+    assert grad <= tol and (par <= tol).all(), (adj, jvp, grad, par)
+
+
+def test_colliders_taped_forward_follows_the_solver(pbf, scenes):
+    pos, vel, mn, mx, prm, _ = scene(scenes, vorticity=1e-4)
+    a = pbf.PBFAdjoint()
+    a.initialize(len(pos), mn, mx, prm, max_neighbors=128, checkpoint_every=3)
+    with_colliders(a)
+    s = with_colliders(pbf.PBFSolver())
+    s.initialize(len(pos), mn, mx, prm)
+    s.set_particles(pos, vel)
+    x, v = a.forward(pos, vel, 1)
+    s.run(1)
+    np.testing.assert_array_equal(x, s.copy_positions_to_host())
+    np.testing.assert_array_equal(v, s.copy_velocities_to_host())
+
+
+def test_colliders_adjoint_matches_fp64_forward_mode(pbf, scenes, orc):
+    pos, vel, mn, mx, prm, target = scene(scenes, vorticity=1e-4)
+    n = len(pos)
+    steps = 6
+    a = pbf.PBFAdjoint()
+    a.initialize(n, mn, mx, prm, max_neighbors=128, checkpoint_every=4)
+    with_colliders(a)
+    x, _ = a.forward(pos, vel, steps)
+    L, gx = loss_grad(x, target)
+    gx0, gv0, gr, gc = a.backward(gx, np.zeros_like(gx))
+    a.close()
+    gv0 = gv0[:, :3].astype(np.float64)
+    rng = np.random.default_rng(23)
+    dirs = rng.standard_normal((4, n, 3))
+    k = 6
+    tv = np.zeros((k, n, 3))
+    tv[:4] = dirs
+    trho = np.array([0.0, 0.0, 0.0, 0.0, 1.0, 0.0])
+    tc = np.array([0.0, 0.0, 0.0, 0.0, 0.0, 1.0])
+    x64, _, txo, _ = orc.diff_rollout(pos, vel, prm.as_dict(), mn, mx, steps, tv0=tv, trho=trho,
+                                      tc=tc, **COLLIDERS)
+    np.testing.assert_allclose(x[:, :3], x64, atol=5e-5, rtol=0)
+    d = (x64 - target) * (2.0 / n)
+    jvp = np.array([(d * txo[q]).sum() for q in range(k)])
+    adj = np.array([(gv0 * dirs[q]).sum() for q in range(4)] + [gr, gc])
+    check_gradient(adj, jvp, 4)
+
+
+def test_colliders_adjoint_matches_fp64_tangents_along_its_trajectory(pbf, scenes, orc):
+    pos, vel, mn, mx, prm, target = scene(scenes, vorticity=1e-4)
+    steps, every = 12, 5
+    n = len(pos)
+    a = pbf.PBFAdjoint()
+    a.initialize(n, mn, mx, prm, max_neighbors=128, checkpoint_every=every)
+    with_colliders(a)
+    states = gpu_states(a, pos, vel, steps)
+    x, _ = a.forward(pos, vel, steps)
+    d = x[:, :3].astype(np.float64) - target
+    gx = np.zeros((n, 4), np.float32)
+    gx[:, :3] = (2.0 / n) * d
+    gx0, gv0, gr, gc = a.backward(gx, np.zeros_like(gx))
+    rng = np.random.default_rng(29)
+    dirs = rng.standard_normal((4, n, 3))
+    k = 6
+    tv = np.zeros((k, n, 3))
+    tv[:4] = dirs
+    trho = np.array([0, 0, 0, 0, 1.0, 0])
+    tc = np.array([0, 0, 0, 0, 0, 1.0])
+    _, _, txo, _ = orc.diff_rollout(pos, vel, prm.as_dict(), mn, mx, steps, tv0=tv, trho=trho,
+                                    tc=tc, states=states, **COLLIDERS)
+    jvp = np.array([(d * (2.0 / n) * txo[q]).sum() for q in range(k)])
+    g = gv0[:, :3].astype(np.float64)
+    adj = np.array([(g * dirs[q]).sum() for q in range(4)] + [gr, gc])
+    check_gradient(adj, jvp, 4)
