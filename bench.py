@@ -556,6 +556,48 @@ def adjoint_bench(pkg, scenes, steps: int, every: int, ndirs: int, fd_steps: int
     }
 
 
+def adjoint_reference_scene(pkg, scenes, frames: int = 10, every: int = 5):
+    """Timing of the adjoint on the reference's own benchmark scene (262,144
+    particles, 2 substeps x 4 iterations, box + sphere, XSPH and vorticity
+    on): `frames` steps forward and back against the solver's own forward.
+    Its accuracy is checked on smaller scenes by the test suite."""
+    pos, vel, mn, mx, prm, col = scenes.reference_benchmark()
+    n = len(pos)
+    a = pkg.PBFAdjoint()
+    a.initialize(n, mn, mx, prm, max_neighbors=128, checkpoint_every=every)
+    a.set_spheres(col["spheres"])
+    a.set_boxes(col["boxes"])
+    x, v = a.forward(pos, vel, frames)  # warm-up (graphs)
+    gx = np.zeros((n, 4), np.float32)
+    gx[:, :3] = (2.0 / n) * (x[:, :3] - pos[:, :3])
+    a.backward(gx, np.zeros_like(gx))
+    cuda_sync()
+    t0 = time.perf_counter()
+    a.forward(pos, vel, frames)
+    cuda_sync()
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    a.backward(gx, np.zeros_like(gx))
+    cuda_sync()
+    t_bwd = time.perf_counter() - t0
+    a.close()
+    s = pkg.PBFSolver()
+    s.initialize(n, mn, mx, prm)
+    s.set_spheres(col["spheres"])
+    s.set_boxes(col["boxes"])
+    s.set_particles(pos, vel)
+    s.run(2)
+    s.set_particles(pos, vel)
+    ms_solver = s.time_frames(frames)
+    s.close()
+    return {"particles": n, "frames": frames, "substeps": prm.substeps,
+            "checkpoint_every": every, "forward_ms": 1000.0 * t_fwd,
+            "backward_ms": 1000.0 * t_bwd, "solver_forward_ms": ms_solver,
+            "adjoint_over_solver_forward": 1000.0 * t_bwd / ms_solver,
+            "workload": "the reference benchmark scene: box + sphere colliders, 2 substeps, "
+                        "XSPH and vorticity confinement on"}
+
+
 def run_reference(args):
     rank, world, local = dist_env()
     if rank != 0:
@@ -752,6 +794,7 @@ def main():
         if world == 1 and not args.no_adjoint:
             line["adjoint"] = adjoint_bench(pkg, scenes, args.adjoint_steps, 10,
                                             args.adjoint_directions)
+            line["adjoint_reference_scene"] = adjoint_reference_scene(pkg, scenes)
         if not args.no_cpu_baseline and world == 1:
             budget = float(os.environ.get("PBF_CPU_SECONDS", "20"))
             line["cpu_baseline"] = cpu_baseline(scene, seconds_budget=budget)

@@ -74,15 +74,15 @@ def child(scene: str, warmup: int, frames: int):
 
 def child_adjoint(steps: int):
     """The profiled adjoint workload: 65,536 particles (64x64x16 dam-break
-    lattice, vorticity off), a `steps`-step forward with one checkpoint
-    segment, then the backward (recompute into the tape, adjoint passes)."""
+    lattice, the 1M dam break's parameters: XSPH and vorticity confinement
+    on), a `steps`-step forward with one checkpoint segment (recorded by the
+    forward), then the backward's adjoint passes."""
     import numpy as np
     pkg = load_pkg()
     scenes = importlib.import_module("fluid_simulator_gb300.scenes")
     nx, ny, nz = 64, 64, 16
     S = scenes.SPACING
     pos, vel, mn, mx, prm, _ = scenes.dam_break(nx, ny, nz, (2 * nx * S, 1.5 * ny * S, 2 * nz * S))
-    prm.vorticityStrength = 0.0
     n = len(pos)
     a = pkg.PBFAdjoint()
     a.initialize(n, mn, mx, prm, max_neighbors=128, checkpoint_every=steps)
