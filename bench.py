@@ -315,6 +315,7 @@ def reference_scene(pkg, scenes, frames: int = 60, reps: int = 5, warmup: int = 
     out = {"particles": n, "substeps": sub, "iterations": prm.solverIterations,
            "frames": frames, "repetitions": reps, "warmup_frames": warmup,
            "ours": summary(ours)}
+    out["ours_cpp_shim"] = shim_driver()
     if not build_ref.available():
         out["reference_cuda"] = {"unavailable": "reference kernels not built"}
         return out
@@ -337,7 +338,32 @@ def reference_scene(pkg, scenes, frames: int = 60, reps: int = 5, warmup: int = 
     out["reference_cuda"] = summary(ref)
     out["speedup"] = (out["ours"]["particle_frames_per_s"]
                       / out["reference_cuda"]["particle_frames_per_s"])
+    if "particle_frames_per_s" in out["ours_cpp_shim"]:
+        out["speedup_cpp_shim"] = (out["ours_cpp_shim"]["particle_frames_per_s"]
+                                   / out["reference_cuda"]["particle_frames_per_s"])
     return out
+
+
+def shim_driver():
+    """The same scene and protocol through the C++ shim, timed like the
+    reference's driver: steady_clock around every synchronous
+    PBFSolver::step() (fluid-simulator_gb300/cpp/reference_scene_bench.cpp)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "_pbf103_build_b", os.path.join(ROOT, "fluid-simulator_gb300", "build.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    try:
+        exe = b.build_shim_bench()
+        r = subprocess.run([exe], capture_output=True, text=True, timeout=600)
+    except (RuntimeError, OSError, subprocess.TimeoutExpired) as e:
+        return {"unavailable": str(e).splitlines()[0][:200]}
+    if r.returncode != 0:
+        return {"unavailable": "driver exited %d: %s" % (r.returncode, r.stderr.strip()[:200])}
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    d["method"] = ("C++ driver on include/pbf103/pbf_solver.hpp: steady_clock around each "
+                   "synchronous step(), median of 5 runs of 60 frames")
+    return d
 
 
 def batched(pkg, scenes, steps: int, warmup: int, per_scene_steps: int):

@@ -76,5 +76,31 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     return LIB_PATH
 
 
+SHIM_BENCH_SRC = os.path.join(PKG_DIR, "cpp", "reference_scene_bench.cpp")
+SHIM_BENCH = os.path.join(BUILD_DIR, "reference_scene_bench")
+
+
+def build_shim_bench(force: bool = False) -> str:
+    """Compile the reference-scene driver (cpp/reference_scene_bench.cpp)
+    against the C++ shim with g++, linked to libpbf103.so; returns its path.
+    Floating-point contraction is off so the scene's coordinates are the
+    single-precision products and sums the reference's driver computes."""
+    lib = build()
+    if (not force and os.path.exists(SHIM_BENCH) and
+            os.path.getmtime(SHIM_BENCH) >= max(os.path.getmtime(lib),
+                                                os.path.getmtime(SHIM_BENCH_SRC))):
+        return SHIM_BENCH
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(nvcc())), "include")
+    tmp = SHIM_BENCH + ".tmp%d" % os.getpid()
+    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-Wall", "-I", INCLUDE, "-I", cuda_inc,
+           SHIM_BENCH_SRC, "-o", tmp, lib, "-Wl,-rpath," + BUILD_DIR]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("g++ failed for %s:\n%s%s" % (SHIM_BENCH_SRC, r.stdout, r.stderr))
+    os.replace(tmp, SHIM_BENCH)
+    return SHIM_BENCH
+
+
 if __name__ == "__main__":
     print(build(force=True, verbose=True))
+    print(build_shim_bench(force=True))

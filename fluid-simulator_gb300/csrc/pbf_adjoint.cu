@@ -1002,6 +1002,7 @@ struct pbf_adjoint {
         cuda_check(cudaStreamSynchronize(stream));
         if (h & kStatusNeighborOverflow)
             fail(PBF_ERR_OVERFLOW, "Particle neighbor count exceeds solver capacity");
+        if (h & kStatusNotConverged) fail(PBF_ERR_RUNTIME, "Collision constraints did not converge");
     }
 
     // `frames` solver steps of `subs` substeps each.

@@ -37,3 +37,39 @@ def test_shim_gpu_scenarios(tmp_path, pbf):
     r = subprocess.run([exe, "gpu"], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stdout + r.stderr
     assert "OK" in r.stdout
+
+
+def _shim_bench(pbf):
+    import importlib.util
+    spec = importlib.util.spec_from_file_location(
+        "_pbf103_build_t", os.path.join(ROOT, "fluid-simulator_gb300", "build.py"))
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    return b.build_shim_bench()
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
+def test_reference_scene_driver_builds_the_same_scene(tmp_path, pbf, scenes):
+    """The C++ driver of the reference benchmark scene (written against the
+    shim) starts from the same particles as the Python scene builder, bit for
+    bit (benchmark/pbf_benchmark.cu:85-114)."""
+    import numpy as np
+    exe = _shim_bench(pbf)
+    out = os.path.join(str(tmp_path), "scene.bin")
+    subprocess.check_call([exe, "--dump", out], timeout=60)
+    got = np.fromfile(out, np.float32).reshape(-1, 4)
+    want = scenes.reference_benchmark()[0]
+    assert got.shape == want.shape
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_reference_scene_driver_runs(pbf):
+    """The shim driver runs the reference benchmark protocol end to end."""
+    import json
+    exe = _shim_bench(pbf)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    d = json.loads(r.stdout.strip().splitlines()[-1])
+    assert d["particles"] == 262144 and d["substeps"] == 2 and len(d["runs_ms"]) == 5
+    assert d["ms_per_frame"] > 0.0
