@@ -784,7 +784,7 @@ def main():
                        "single GPU", "l2": "step working set ~250 MB > 129 MB L2 (no flush)",
                        "timing": "CUDA events around %d graph-replayed steps on the solver "
                                  "stream" % args.steps,
-                       "block_sizes": tuned},
+                       "block_sizes": tuned, "walk_lanes": s.walk_lanes()},
             "clocks": clocks,
             "e2e": {"value": e2e_value, "unit": UNIT,
                     "h2d_bytes_per_step": int(2 * 16 * n), "d2h_bytes_per_step": int(2 * 16 * n),

@@ -192,6 +192,8 @@ def _declare(L):
         "pbf_batch_scene_count": ([_vp], C.c_int),
         "pbf_autotune": ([_vp, C.c_int], S),
         "pbf_block_sizes": ([_vp, C.POINTER(C.c_int), C.c_int], S),
+        "pbf_walk_lanes": ([_vp, C.POINTER(C.c_int)], S),
+        "pbf_set_walk_lanes": ([_vp, C.c_int], S),
         "pbf_adjoint_create": ([C.POINTER(_vp), C.c_int], S),
         "pbf_adjoint_destroy": ([_vp], None),
         "pbf_adjoint_last_error": ([_vp], C.c_char_p),
@@ -380,7 +382,8 @@ class PBFSolver:
                      "confine")
 
     def autotune(self, frames_per_trial: int = 2) -> dict:
-        """pbf_autotune: choose the neighbour kernels' block sizes; returns them."""
+        """pbf_autotune: choose the neighbour kernels' block sizes (returned)
+        and the lanes per particle of the walks (walk_lanes())."""
         self._check(self._L.pbf_autotune(self._h, int(frames_per_trial)))
         return self.block_sizes()
 
@@ -388,6 +391,16 @@ class PBFSolver:
         out = (C.c_int * 6)()
         self._check(self._L.pbf_block_sizes(self._h, out, 6))
         return dict(zip(self.TUNED_KERNELS, list(out)))
+
+    def walk_lanes(self) -> int:
+        """Lanes per particle of the list-writing walks (pbf_walk_lanes)."""
+        k = C.c_int()
+        self._check(self._L.pbf_walk_lanes(self._h, C.byref(k)))
+        return k.value
+
+    def set_walk_lanes(self, lanes: int):
+        """pbf_set_walk_lanes: 1, 2 or 4 lanes per particle, 0 = default."""
+        self._check(self._L.pbf_set_walk_lanes(self._h, int(lanes)))
 
     def set_particles(self, positions, velocities, count: Optional[int] = None):
         if positions is None or velocities is None:

@@ -761,6 +761,7 @@ struct pbf_adjoint {
         c.vort_eps = p.vorticityStrength;
         c.max_nb = max_nb;
         c.stride = stride;
+        c.walk_lanes = default_walk_lanes(n, max_nb);
         c.col.cminx = lo.x;
         c.col.cminy = lo.y;
         c.col.cminz = lo.z;

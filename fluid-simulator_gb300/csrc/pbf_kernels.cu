@@ -262,13 +262,16 @@ __device__ __forceinline__ float lambda_finish(const StepConst& c, const LambdaA
 }
 
 // The neighbour walk of particle i (position pi): writes the list slot-major
-// at out[slot * stride] (at most max_nb entries) and returns the full count.
-// STORE = false counts the hits without writing the list.
-template <bool B, bool STORE = true>
+// at out[slot * stride] (at most cap entries) and returns the full count.
+// STORE = false counts the hits without writing the list.  With PARTS > 1
+// only rows [part * rows / PARTS, (part + 1) * rows / PARTS) of the stencil
+// are walked (rows in z -> y order), so the lists of parts 0, 1, ...
+// concatenated are the whole list.  (PARTS = parts.)
+template <bool B, bool STORE = true, int PARTS = 1>
 __device__ __forceinline__ int walk(const StepConst& c, int i, float4 pi,
                                     const float* __restrict__ sx, const float* __restrict__ sy,
                                     const float* __restrict__ sz, const int* __restrict__ first,
-                                    uint32_t* __restrict__ out) {
+                                    uint32_t* __restrict__ out, int cap, int part = 0) {
     GridConst g;
     uint32_t base;
     grid_of<B>(c, i, g, base);
@@ -283,7 +286,6 @@ __device__ __forceinline__ int walk(const StepConst& c, int i, float4 pi,
     const uint32_t gx = static_cast<uint32_t>(g.gx);
     const uint32_t gxy = gx * static_cast<uint32_t>(g.gy);
     const float h2 = c.k.h2;
-    const int max_nb = c.max_nb;
     const size_t stride = nb_step(c);
     const f32x2 px = pack2(pi.x, pi.x), py = pack2(pi.y, pi.y), pz = pack2(pi.z, pi.z);
     int count = 0;
@@ -296,50 +298,123 @@ __device__ __forceinline__ int walk(const StepConst& c, int i, float4 pi,
     // and the hits are then appended in ascending order.  Candidates outside
     // [s, e) and the particle itself are masked off; the component arrays
     // are padded so the odd element past e is always readable.
-    for (int z = z0; z <= z1; ++z) {
-        for (int y = y0; y <= y1; ++y) {
-            const uint32_t row =
-                base + static_cast<uint32_t>(y) * gx + static_cast<uint32_t>(z) * gxy;
-            const int s = __ldg(&first[row + static_cast<uint32_t>(x0)]);
-            const int e = __ldg(&first[row + static_cast<uint32_t>(x1) + 1u]);
-            for (int j0 = s & ~1; j0 < e; j0 += 32) {
-                const int lim = min(32, e - j0);
-                uint32_t mask = 0u;
+    auto row_walk = [&](int z, int y) {
+        const uint32_t row =
+            base + static_cast<uint32_t>(y) * gx + static_cast<uint32_t>(z) * gxy;
+        const int s = __ldg(&first[row + static_cast<uint32_t>(x0)]);
+        const int e = __ldg(&first[row + static_cast<uint32_t>(x1) + 1u]);
+        for (int j0 = s & ~1; j0 < e; j0 += 32) {
+            const int lim = min(32, e - j0);
+            uint32_t mask = 0u;
 #pragma unroll 4
-                for (int b = 0; b < lim; b += 2) {
-                    const float2 X = __ldg(reinterpret_cast<const float2*>(sx + j0 + b));
-                    const float2 Y = __ldg(reinterpret_cast<const float2*>(sy + j0 + b));
-                    const float2 Z = __ldg(reinterpret_cast<const float2*>(sz + j0 + b));
-                    const f32x2 d2 = dist2x2(sub2(px, pack2(X.x, X.y)),
-                                             sub2(py, pack2(Y.x, Y.y)),
-                                             sub2(pz, pack2(Z.x, Z.y)));
-                    float da, db;
-                    unpack2(d2, da, db);
-                    mask |= (static_cast<uint32_t>(da <= h2) |
-                             (static_cast<uint32_t>(db <= h2) << 1)) << b;
+            for (int b = 0; b < lim; b += 2) {
+                const float2 X = __ldg(reinterpret_cast<const float2*>(sx + j0 + b));
+                const float2 Y = __ldg(reinterpret_cast<const float2*>(sy + j0 + b));
+                const float2 Z = __ldg(reinterpret_cast<const float2*>(sz + j0 + b));
+                const f32x2 d2 = dist2x2(sub2(px, pack2(X.x, X.y)),
+                                         sub2(py, pack2(Y.x, Y.y)),
+                                         sub2(pz, pack2(Z.x, Z.y)));
+                float da, db;
+                unpack2(d2, da, db);
+                mask |= (static_cast<uint32_t>(da <= h2) |
+                         (static_cast<uint32_t>(db <= h2) << 1)) << b;
+            }
+            // Keep bits of [s, e) only, and drop the particle itself.
+            uint32_t valid = lim >= 32 ? 0xffffffffu : ((1u << lim) - 1u);
+            if (j0 < s) valid &= ~((1u << (s - j0)) - 1u);
+            const int self = i - j0;
+            if (self >= 0 && self < 32) valid &= ~(1u << self);
+            mask &= valid;
+            if constexpr (STORE) {
+                while (mask) {
+                    const int b = __ffs(mask) - 1;
+                    mask &= mask - 1u;
+                    if (count < cap)
+                        out[static_cast<size_t>(count) * stride] =
+                            static_cast<uint32_t>(j0 + b);
+                    ++count;
                 }
-                // Keep bits of [s, e) only, and drop the particle itself.
-                uint32_t valid = lim >= 32 ? 0xffffffffu : ((1u << lim) - 1u);
-                if (j0 < s) valid &= ~((1u << (s - j0)) - 1u);
-                const int self = i - j0;
-                if (self >= 0 && self < 32) valid &= ~(1u << self);
-                mask &= valid;
-                if constexpr (STORE) {
-                    while (mask) {
-                        const int b = __ffs(mask) - 1;
-                        mask &= mask - 1u;
-                        if (count < max_nb)
-                            out[static_cast<size_t>(count) * stride] =
-                                static_cast<uint32_t>(j0 + b);
-                        ++count;
-                    }
-                } else {
-                    count += __popc(mask);
-                }
+            } else {
+                count += __popc(mask);
+            }
+        }
+    };
+    if constexpr (PARTS == 1) {
+        for (int z = z0; z <= z1; ++z)
+            for (int y = y0; y <= y1; ++y) row_walk(z, y);
+    } else {
+        const int ny = y1 - y0 + 1;
+        const int rows = ny * (z1 - z0 + 1);
+        const int r_end = (part + 1) * rows / PARTS;
+        int r = part * rows / PARTS;
+        int z = z0 + r / ny, y = y0 + r % ny;
+        for (; r < r_end; ++r) {
+            row_walk(z, y);
+            if (++y > y1) {
+                y = y0;
+                ++z;
             }
         }
     }
     return count;
+}
+
+// Second pass over the list just written: the constraint terms run once per
+// neighbour instead of once per candidate in which any lane of the warp hit.
+// Same order as the list, so the same sums.  Neighbours are taken two at a
+// time with FP32x2 arithmetic; the sums stay in list order.  The next pair's
+// indices are loaded before this pair is gathered.
+template <bool B>
+__device__ __forceinline__ float lambda_of_list(const StepConst& c, int i, float4 pi,
+                                                const float4* __restrict__ xs,
+                                                const uint32_t* __restrict__ out, size_t stride,
+                                                int count) {
+    const f32x2 px = pack2(pi.x, pi.x), py = pack2(pi.y, pi.y), pz = pack2(pi.z, pi.z);
+    LambdaAcc acc{c.k.c_poly6, 0.0f, 0.0f, 0.0f, 0.0f};
+    int k = 0;
+    uint32_t na = 0u, nb2 = 0u;
+    if (count >= 2) {
+        na = out[0];
+        nb2 = out[stride];
+    }
+    for (; k + 2 <= count; k += 2) {
+        const uint32_t ja = na, jb = nb2;
+        if (k + 4 <= count) {
+            na = out[static_cast<size_t>(k + 2) * stride];
+            nb2 = out[static_cast<size_t>(k + 3) * stride];
+        }
+        const float4 a = __ldg(&xs[ja]);
+        const float4 b = __ldg(&xs[jb]);
+        const f32x2 dx = sub2(px, pack2(a.x, b.x));
+        const f32x2 dy = sub2(py, pack2(a.y, b.y));
+        const f32x2 dz = sub2(pz, pack2(a.z, b.z));
+        lambda_add2(c.k, acc, dx, dy, dz, dist2x2(dx, dy, dz));
+    }
+    if (k < count) {
+        const float4 pj = __ldg(&xs[out[static_cast<size_t>(k) * stride]]);
+        const float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y), dz = fsub(pi.z, pj.z);
+        lambda_add(c.k, acc, dx, dy, dz, dist2(dx, dy, dz));
+    }
+    if constexpr (B) {
+        const SceneConst& sc = scene_of(c, i);
+        return lambda_finish(sc.mass, sc.rho0, sc.gs2, c.lambda_eps, acc);
+    } else {
+        return lambda_finish(c, acc);
+    }
+}
+
+// What k_search does once particle i's list (count entries) is written.
+template <bool LAMBDA, bool B>
+__device__ __forceinline__ void search_tail(const StepConst& c, int i, float4 pi,
+                                            const float4* __restrict__ xs,
+                                            const uint32_t* __restrict__ out, int count,
+                                            int* __restrict__ cnt, float* __restrict__ lam,
+                                            unsigned* __restrict__ status) {
+    cnt[i] = count;
+    if (count > c.max_nb) atomicOr(status, kStatusNeighborOverflow);
+    if (LAMBDA)
+        lam[i] = count > c.max_nb ? CUDART_NAN_F
+                                  : lambda_of_list<B>(c, i, pi, xs, out, nb_step(c), count);
 }
 
 template <bool LAMBDA, bool B>
@@ -352,55 +427,83 @@ k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
     if (i >= n || fatal(status)) return;
     const float4 pi = xs[i];
     uint32_t* __restrict__ out = nbr + nb_first(c, i);
-    const int count = walk<B>(c, i, pi, sx, sy, sz, first, out);
-    const int max_nb = c.max_nb;
+    const int count = walk<B>(c, i, pi, sx, sy, sz, first, out, c.max_nb);
+    search_tail<LAMBDA, B>(c, i, pi, xs, out, count, cnt, lam, status);
+}
+
+// Split walk: the L lanes of a group (consecutive lanes, gmask) walk
+// consecutive parts of particle i's stencil rows.  Part `sub` writes its hits
+// into slots [sub * P, (sub + 1) * P) of the particle's slot-major list
+// (P = max_nb / L); the parts are then moved down to their final slots in
+// part order, so the list is the one walk<B> writes, entry for entry.  If a
+// part holds more than P hits (and the whole list fits), lane 0 walks all
+// rows again.  Returns the full count on every lane of the group.
+template <bool B, int L>
+__device__ __forceinline__ int walk_split(const StepConst& c, int i, int sub, unsigned gmask,
+                                          float4 pi, const float* __restrict__ sx,
+                                          const float* __restrict__ sy,
+                                          const float* __restrict__ sz,
+                                          const int* __restrict__ first,
+                                          uint32_t* __restrict__ out) {
+    const int P = c.max_nb / L;
     const size_t stride = nb_step(c);
-    const f32x2 px = pack2(pi.x, pi.x), py = pack2(pi.y, pi.y), pz = pack2(pi.z, pi.z);
-    cnt[i] = count;
-    if (count > max_nb) atomicOr(status, kStatusNeighborOverflow);
-    if (LAMBDA) {
-        if (count > max_nb) {
-            lam[i] = CUDART_NAN_F;
-            return;
-        }
-        // Second pass over the list just written: the constraint terms run
-        // once per neighbour instead of once per candidate in which any lane
-        // of the warp hit.  Same order as the list, so the same sums.
-        // Neighbours are taken two at a time with FP32x2 arithmetic; the sums
-        // stay in list order.
-        // The next pair's indices are loaded before this pair is gathered.
-        LambdaAcc acc{c.k.c_poly6, 0.0f, 0.0f, 0.0f, 0.0f};
-        int k = 0;
-        uint32_t na = 0u, nb2 = 0u;
-        if (count >= 2) {
-            na = out[0];
-            nb2 = out[stride];
-        }
-        for (; k + 2 <= count; k += 2) {
-            const uint32_t ja = na, jb = nb2;
-            if (k + 4 <= count) {
-                na = out[static_cast<size_t>(k + 2) * stride];
-                nb2 = out[static_cast<size_t>(k + 3) * stride];
-            }
-            const float4 a = __ldg(&xs[ja]);
-            const float4 b = __ldg(&xs[jb]);
-            const f32x2 dx = sub2(px, pack2(a.x, b.x));
-            const f32x2 dy = sub2(py, pack2(a.y, b.y));
-            const f32x2 dz = sub2(pz, pack2(a.z, b.z));
-            lambda_add2(c.k, acc, dx, dy, dz, dist2x2(dx, dy, dz));
-        }
-        if (k < count) {
-            const float4 pj = __ldg(&xs[out[static_cast<size_t>(k) * stride]]);
-            const float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y), dz = fsub(pi.z, pj.z);
-            lambda_add(c.k, acc, dx, dy, dz, dist2(dx, dy, dz));
-        }
-        if constexpr (B) {
-            const SceneConst& sc = scene_of(c, i);
-            lam[i] = lambda_finish(sc.mass, sc.rho0, sc.gs2, c.lambda_eps, acc);
-        } else {
-            lam[i] = lambda_finish(c, acc);
-        }
+    const int mine = walk<B, true, L>(c, i, pi, sx, sy, sz, first,
+                                      out + static_cast<size_t>(sub) * P * stride, P, sub);
+    __syncwarp(gmask);  // every part's stores ordered before any rewrite
+    int incl = mine;
+#pragma unroll
+    for (int d = 1; d < L; d <<= 1) {
+        const int v = __shfl_up_sync(gmask, incl, d, L);
+        if (sub >= d) incl += v;
     }
+    const int total = __shfl_sync(gmask, incl, L - 1, L);
+    const bool spill = __any_sync(gmask, mine > P);
+    if (total > c.max_nb) return total;  // overflow: the list is not read
+    if (spill) {
+        if (sub == 0) walk<B>(c, i, pi, sx, sy, sz, first, out, c.max_nb);
+        __syncwarp(gmask);
+        return total;
+    }
+    // Part s's final slots end at or below slot s * P, where part s + 1's
+    // hits start, so moving the parts in order never overwrites hits not yet
+    // moved.
+    const int excl = incl - mine;
+#pragma unroll
+    for (int s = 1; s < L; ++s) {
+        if (sub == s)
+            for (int k = 0; k < mine; ++k)
+                out[static_cast<size_t>(excl + k) * stride] =
+                    out[static_cast<size_t>(s * P + k) * stride];
+        __syncwarp(gmask);
+    }
+    return total;
+}
+
+template <int L>
+__device__ __forceinline__ unsigned lane_group_mask() {
+    const unsigned lane = threadIdx.x & 31u;
+    return ((1u << L) - 1u) << (lane & ~(L - 1u));
+}
+
+// k_search with L lanes per particle for the walk (slot-major lists only);
+// lane 0 of each group computes lambda.  For scenes too small to fill the
+// GPU with one thread per particle, where a walk is bound by the latency of
+// one thread's row after row.
+template <bool LAMBDA, bool B, int L>
+__global__ void __launch_bounds__(kMaxTunedBlock)
+k_search_split(const float4* __restrict__ xs, const float* __restrict__ sx,
+               const float* __restrict__ sy, const float* __restrict__ sz,
+               const int* __restrict__ first, StepConst c, int n, uint32_t* __restrict__ nbr,
+               int* __restrict__ cnt, float* __restrict__ lam, unsigned* __restrict__ status) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = t / L, sub = t % L;
+    if (i >= n) return;  // whole groups
+    const unsigned gmask = lane_group_mask<L>();
+    if (__any_sync(gmask, fatal(status))) return;
+    const float4 pi = xs[i];
+    uint32_t* __restrict__ out = nbr + nb_first(c, i);
+    const int count = walk_split<B, L>(c, i, sub, gmask, pi, sx, sy, sz, first, out);
+    if (sub == 0) search_tail<LAMBDA, B>(c, i, pi, xs, out, count, cnt, lam, status);
 }
 
 // Compact lists, first pass: the walk's neighbour count only.
@@ -412,7 +515,7 @@ k_count(const float4* __restrict__ xs, const float* __restrict__ sx,
         unsigned* __restrict__ status) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || fatal(status)) return;
-    const int count = walk<B, false>(c, i, xs[i], sx, sy, sz, first, nullptr);
+    const int count = walk<B, false>(c, i, xs[i], sx, sy, sz, first, nullptr, c.max_nb);
     cnt[i] = count;
     if (count > c.max_nb) atomicOr(status, kStatusNeighborOverflow);
 }
@@ -749,6 +852,24 @@ k_xsph(const float4* __restrict__ x, const float4* __restrict__ v,
     v_out[i] = out;
 }
 
+// What the final walk does once particle i's list (count entries) is written.
+template <bool B>
+__device__ __forceinline__ void xsph_tail(const StepConst& c, int i, float4 pi,
+                                          const float4* __restrict__ xs,
+                                          const uint32_t* __restrict__ nbr, int count,
+                                          int* __restrict__ cnt, const float4* __restrict__ v,
+                                          float4* __restrict__ v_out,
+                                          const float4* __restrict__ vin, bool resolve,
+                                          unsigned* __restrict__ status) {
+    cnt[i] = count;
+    if (count > c.max_nb) atomicOr(status, kStatusNeighborOverflow);
+    float4 out = xsph_one(c, xs, v, nbr, count, i, B ? scene_of(c, i).xsph_c : c.xsph_c);
+    if (resolve)
+        resolve_velocity(colliders_of<B>(c, i), c.particle_radius, c.restitution, c.friction,
+                         pi, vin[i], out);
+    v_out[i] = out;
+}
+
 // The final rebuild's walk with XSPH fused in: the list is written, then
 // applyXsphViscosity runs over it in a second pass (velocities v are the
 // updated ones, computed before this walk), with the velocity response when
@@ -763,14 +884,29 @@ k_search_xsph(const float4* __restrict__ xs, const float* __restrict__ sx,
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || fatal(status)) return;
     const float4 pi = xs[i];
-    const int count = walk<B>(c, i, pi, sx, sy, sz, first, nbr + nb_first(c, i));
-    cnt[i] = count;
-    if (count > c.max_nb) atomicOr(status, kStatusNeighborOverflow);
-    float4 out = xsph_one(c, xs, v, nbr, count, i, B ? scene_of(c, i).xsph_c : c.xsph_c);
-    if (resolve)
-        resolve_velocity(colliders_of<B>(c, i), c.particle_radius, c.restitution, c.friction,
-                         pi, vin[i], out);
-    v_out[i] = out;
+    const int count = walk<B>(c, i, pi, sx, sy, sz, first, nbr + nb_first(c, i), c.max_nb);
+    xsph_tail<B>(c, i, pi, xs, nbr, count, cnt, v, v_out, vin, resolve, status);
+}
+
+// k_search_xsph with L lanes per particle for the walk; lane 0 of each group
+// applies XSPH (see k_search_split).
+template <bool B, int L>
+__global__ void __launch_bounds__(kMaxTunedBlock)
+k_search_xsph_split(const float4* __restrict__ xs, const float* __restrict__ sx,
+                    const float* __restrict__ sy, const float* __restrict__ sz,
+                    const int* __restrict__ first, StepConst c, int n,
+                    uint32_t* __restrict__ nbr, int* __restrict__ cnt,
+                    const float4* __restrict__ v, float4* __restrict__ v_out,
+                    const float4* __restrict__ vin, bool resolve, unsigned* __restrict__ status) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = t / L, sub = t % L;
+    if (i >= n) return;  // whole groups
+    const unsigned gmask = lane_group_mask<L>();
+    if (__any_sync(gmask, fatal(status))) return;
+    const float4 pi = xs[i];
+    const int count =
+        walk_split<B, L>(c, i, sub, gmask, pi, sx, sy, sz, first, nbr + nb_first(c, i));
+    if (sub == 0) xsph_tail<B>(c, i, pi, xs, nbr, count, cnt, v, v_out, vin, resolve, status);
 }
 
 // computeVorticity (pbf_solver_kernels.cu:268-315).
@@ -1044,10 +1180,59 @@ void launch_gather_first(const uint32_t* perm, const float4* xs_in, float4* xs_o
 }
 inline int tuned_block(const StepConst& c, int k) { return c.blk[k] > 0 ? c.blk[k] : kBlock; }
 
+// Scene size below which the walks split each particle's rows over 4 lanes
+// by default.  Measured per walk + lambda launch (1 / 2 / 4 lanes): 43.5 /
+// 36.9 / 35.7 us at 16,384 particles, 40.2 / 45.8 / 61.4 us at 65,536 (from
+// there on lane 0's lambda pass, alone in its group, costs more than the
+// split walk saves).
+constexpr size_t kSplitWalk4Below = size_t(1) << 15;
+
+// Lanes per particle of a launch: c.walk_lanes where the split walk applies.
+inline int split_lanes(const StepConst& c, int n) {
+    const int L = c.walk_lanes;
+    if ((L != 2 && L != 4) || c.nb_off != nullptr || c.max_nb < L ||
+        static_cast<long long>(n) * L > (1LL << 30))
+        return 1;
+    return L;
+}
+
+int default_walk_lanes(size_t n, int max_nb) {
+    const int L = n < kSplitWalk4Below ? 4 : 1;
+    return max_nb >= L ? L : 1;
+}
+
+template <bool LAMBDA, bool B>
+void launch_search_split(int L, int bs, const float4* xs, const float* sx, const float* sy,
+                         const float* sz, const int* first, const StepConst& c, int n,
+                         uint32_t* nbr, int* cnt, float* lam, unsigned* status, cudaStream_t st) {
+    const unsigned g = blocks_for(static_cast<size_t>(n) * L, bs);
+    if (L == 4)
+        launch_k(k_search_split<LAMBDA, B, 4>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr, cnt,
+                 lam, status);
+    else
+        launch_k(k_search_split<LAMBDA, B, 2>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr, cnt,
+                 lam, status);
+}
+
 void launch_search(const float4* xs, const float* sx, const float* sy, const float* sz,
                    const int* first, const StepConst& c, int n, uint32_t* nbr, int* cnt, float* lam,
                    unsigned* status, bool with_lambda, cudaStream_t st) {
     const int bs = tuned_block(c, with_lambda ? kTunedSearchLambda : kTunedSearch);
+    if (const int L = split_lanes(c, n); L > 1) {
+        if (with_lambda && c.scenes)
+            launch_search_split<true, true>(L, bs, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
+                                            status, st);
+        else if (with_lambda)
+            launch_search_split<true, false>(L, bs, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
+                                             status, st);
+        else if (c.scenes)
+            launch_search_split<false, true>(L, bs, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
+                                             status, st);
+        else
+            launch_search_split<false, false>(L, bs, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
+                                              status, st);
+        return;
+    }
     const unsigned g = blocks_for(n, bs);
     if (with_lambda && c.scenes)
         launch_k(k_search<true, true>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr, cnt, lam,
@@ -1068,6 +1253,22 @@ void launch_search_xsph(const float4* xs, const float* sx, const float* sy, cons
                         const float4* v, float4* v_out, const float4* vin, bool resolve,
                         unsigned* status, cudaStream_t st) {
     const int bs = tuned_block(c, kTunedSearch);
+    if (const int L = split_lanes(c, n); L > 1) {
+        const unsigned g = blocks_for(static_cast<size_t>(n) * L, bs);
+        if (c.scenes && L == 4)
+            launch_k(k_search_xsph_split<true, 4>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr,
+                     cnt, v, v_out, vin, resolve, status);
+        else if (c.scenes)
+            launch_k(k_search_xsph_split<true, 2>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr,
+                     cnt, v, v_out, vin, resolve, status);
+        else if (L == 4)
+            launch_k(k_search_xsph_split<false, 4>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr,
+                     cnt, v, v_out, vin, resolve, status);
+        else
+            launch_k(k_search_xsph_split<false, 2>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr,
+                     cnt, v, v_out, vin, resolve, status);
+        return;
+    }
     const unsigned g = blocks_for(n, bs);
     if (c.scenes)
         launch_k(k_search_xsph<true>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr, cnt, v, v_out,

@@ -43,7 +43,15 @@ struct StepConst {
     // nb_cap entries.  Null: slot-major lists, nbr[k * stride + i].
     const uint32_t* nb_off;
     size_t nb_cap;
+    // Lanes per particle in the list-writing walks (1, 2 or 4; 0 = 1): more
+    // than one splits each particle's stencil rows over a lane group, for
+    // scenes too small to fill the GPU.  Slot-major lists only.
+    int walk_lanes;
 };
+
+// Lanes per particle for the walks of an n-particle scene (slot-major lists
+// with max_nb slots).
+int default_walk_lanes(size_t n, int max_nb);
 
 // Kernels whose block size the solver's autotuner chooses.
 enum TunedKernel { kTunedSearchLambda, kTunedDelta, kTunedSearch, kTunedXsph, kTunedVorticity,

@@ -199,6 +199,7 @@ struct pbf_solver {
 
     // Threads per block of the tuned kernels (0 = the default 256).
     int tuned[kTunedCount] = {};
+    int tuned_lanes = 0;  // lanes per particle of the walks chosen by autotune; 0 = default
 
     // Compact neighbour lists (list_cap > 0): every rebuild counts the
     // neighbours, scans the counts into nb_off and writes each particle's
@@ -304,6 +305,7 @@ struct pbf_solver {
             c.nb_off = nb_off.as<uint32_t>();
             c.nb_cap = list_cap;
         }
+        c.walk_lanes = walk_lanes();
         return c;
     }
 
@@ -551,10 +553,12 @@ struct pbf_solver {
         std::vector<int> launches(kStageCount);
         int saved[kTunedCount];
         std::copy(tuned, tuned + kTunedCount, saved);
+        const int saved_lanes = tuned_lanes;
         try {
             tune_all(frames_per_trial, ms, launches, sx.as<float4>(), sv.as<float4>());
         } catch (...) {
             std::copy(saved, saved + kTunedCount, tuned);
+            tuned_lanes = saved_lanes;
             clear_graphs();
             set_particles(sx.as<float4>(), sv.as<float4>(), n, true);
             throw;
@@ -591,6 +595,35 @@ struct pbf_solver {
             }
             tuned[k] = best;
         }
+        // Lanes per particle of the two list-writing walks, timed together.
+        if (list_cap > 0) return;
+        int best = walk_lanes();
+        float best_ms = -1.0f;
+        for (int L : {1, 2, 4}) {
+            if (max_nb < L) continue;
+            tuned_lanes = L;
+            clear_graphs();
+            float t = -1.0f;
+            for (int f = 0; f < frames_per_trial; ++f) {
+                set_particles(x0, v0, n, true);
+                profile_frame(ms.data(), launches.data());
+                const float v = ms[kStSearchLambda] + ms[kStSearch];
+                t = t < 0.0f ? v : std::min(t, v);
+            }
+            if (best_ms < 0.0f || t < best_ms) {
+                best_ms = t;
+                best = L;
+            }
+        }
+        tuned_lanes = best;
+    }
+
+    // Lanes per particle of the list-writing walks: the tuned value, else
+    // the default for the scene size; 1 with compact lists.
+    int walk_lanes() const {
+        if (list_cap > 0) return 1;
+        const int L = tuned_lanes > 0 ? tuned_lanes : default_walk_lanes(n, max_nb);
+        return max_nb >= L && n * size_t(L) <= (size_t(1) << 30) ? L : 1;
     }
 
     void check_status() {
@@ -1109,6 +1142,24 @@ pbf_status pbf_block_sizes(const pbf_solver* s, int* sizes, int count) {
     }
     for (int k = 0; k < count && k < kTunedCount; ++k)
         sizes[k] = s->tuned[k] > 0 ? s->tuned[k] : kBlock;
+    return PBF_OK;
+}
+
+pbf_status pbf_set_walk_lanes(pbf_solver* s, int lanes) {
+    PBF_GUARD(s, {
+        if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4)
+            fail(PBF_ERR_INVALID_ARGUMENT, "walk lanes must be 0, 1, 2 or 4");
+        s->tuned_lanes = lanes;
+        s->clear_graphs();
+    });
+}
+
+pbf_status pbf_walk_lanes(const pbf_solver* s, int* lanes) {
+    if (!s || !lanes) {
+        pbf::set_global_error("solver handle and lanes must not be null");
+        return PBF_ERR_INVALID_ARGUMENT;
+    }
+    *lanes = s->walk_lanes();
     return PBF_OK;
 }
 

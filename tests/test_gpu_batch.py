@@ -83,8 +83,10 @@ def test_autotune_keeps_results_and_state(pbf, scenes):
     a.set_particles(pos, vel)
     a.run(3)
     x0, v0 = a.copy_positions_to_host(), a.copy_velocities_to_host()
+    assert a.walk_lanes() == 4  # default below 32,768 particles
     sizes = a.autotune(1)
     assert set(sizes.values()) <= {128, 256, 512}
+    assert a.walk_lanes() in (1, 2, 4)
     np.testing.assert_array_equal(a.copy_positions_to_host(), x0)
     np.testing.assert_array_equal(a.copy_velocities_to_host(), v0)
     a.run(4)
@@ -94,3 +96,23 @@ def test_autotune_keeps_results_and_state(pbf, scenes):
     b.run(4)
     np.testing.assert_array_equal(a.copy_positions_to_host(), b.copy_positions_to_host())
     np.testing.assert_array_equal(a.copy_velocities_to_host(), b.copy_velocities_to_host())
+
+
+@pytest.mark.parametrize("lanes", [1, 2, 4])
+def test_walk_lanes_change_no_result(pbf, scenes, orc, lanes):
+    """Splitting each particle's stencil rows over 1, 2 or 4 lanes writes the
+    same lists: steps stay bit for bit those of the FP32 oracle."""
+    pos, vel, mn, mx, prm, _ = scenes.dam_break_16k()
+    s = pbf.PBFSolver()
+    s.initialize(len(pos), mn, mx, prm)
+    s.set_walk_lanes(lanes)
+    assert s.walk_lanes() == lanes
+    s.set_particles(pos, vel)
+    s.run(3)
+    o = orc.OracleSolver(32)
+    o.initialize(len(pos), mn, mx, prm.as_dict())
+    o.set_particles(pos, vel)
+    assert o.run(3) == 0
+    assert np.array_equal(s.copy_positions_to_host().view(np.uint32), o.positions().view(np.uint32))
+    assert np.array_equal(s.copy_velocities_to_host().view(np.uint32),
+                          o.velocities().view(np.uint32))

@@ -170,3 +170,28 @@ def test_neighbor_lists_bit_exact_vs_oracle_slot_order(pbf, scenes, orc):
     for k in range(kmax):
         used = cnt > k
         assert_bitwise(nb[k * n:(k + 1) * n][used], onb[k * n:(k + 1) * n][used], "slot %d" % k)
+
+
+def test_split_walk_part_overflow_falls_back(pbf, scenes, orc):
+    """Small scenes split each particle's stencil rows over lanes, each part
+    writing into its share of the list slots; when all neighbours lie in one
+    row (a line of particles along x) one part overflows its share while the
+    whole list fits, and the particle is walked again in one lane.  The
+    result is the one-lane result, bit for bit."""
+    k = 200
+    pos = np.ones((k, 4), np.float32)
+    pos[:, 0] = np.float32(0.05) + np.arange(k, dtype=np.float32) * np.float32(0.02)
+    pos[:, 1] = np.float32(0.3)
+    pos[:, 2] = np.float32(0.3)
+    vel = np.zeros_like(pos)
+    prm = scenes.dam_break_params()
+    s, o = make_pair(pbf, orc, (pos, vel, (0.0, 0.0, 0.0), (4.2, 1.0, 1.0), prm, {}),
+                     max_neighbors=32)
+    s.run(3)
+    assert o.run(3) == 0
+    assert_bitwise(s.copy_positions_to_host(), o.positions(), "positions")
+    assert_bitwise(s.copy_velocities_to_host(), o.velocities(), "velocities")
+    wp, wid, wcnt = s.working_state()
+    op, oid, ocnt = o.working()
+    assert wcnt.max() > 32 // 4, "the scene must overflow one part's share of slots"
+    assert_bitwise(wcnt, ocnt, "neighbour counts")
