@@ -63,6 +63,21 @@ def build_if_possible() -> bool:
     return available()
 
 
+def compile_benchmark_on_shim(lib_path: str, include_dir: str, out_path: str) -> bool:
+    """Compiles the reference's benchmark driver (benchmark/pbf_benchmark.cu),
+    unmodified, against this repository's C++ shim (include_dir/compat puts
+    the shim at "pbf/pbf_solver.hpp") and links lib_path.  Returns False when
+    the reference tree is absent.  A build check: the binary is not run."""
+    src = os.path.join(REFERENCE, "benchmark", "pbf_benchmark.cu")
+    if not os.path.exists(src):
+        return False
+    subprocess.check_call([nvcc(), "-std=c++17", "-O2", "-gencode", "arch=compute_103a,code=sm_103a",
+                           "-I", os.path.join(include_dir, "compat"), "-I", include_dir, src,
+                           "-o", out_path, lib_path, "-Xlinker",
+                           "-rpath=" + os.path.dirname(lib_path)])
+    return True
+
+
 if __name__ == "__main__":
     build(force=True)
     print("\n".join(fatbin_path(u) for u in UNITS))

@@ -73,3 +73,17 @@ def test_reference_scene_driver_runs(pbf):
     d = json.loads(r.stdout.strip().splitlines()[-1])
     assert d["particles"] == 262144 and d["substeps"] == 2 and len(d["runs_ms"]) == 5
     assert d["ms_per_frame"] > 0.0
+
+
+def test_reference_benchmark_builds_unchanged_on_the_shim(tmp_path, pbf):
+    """The reference's own benchmark driver compiles, unmodified, against the
+    shim through the forwarding header include/compat/pbf/pbf_solver.hpp and
+    links libpbf103.so (needs the reference tree; a build check only)."""
+    import sys
+    sys.path.insert(0, ROOT)
+    from oracle import build_ref
+    out = os.path.join(str(tmp_path), "pbf_benchmark_on_shim")
+    if not build_ref.compile_benchmark_on_shim(pbf.library_path(), os.path.join(ROOT, "include"),
+                                               out):
+        pytest.skip("reference tree not present")
+    assert os.path.exists(out)
