@@ -5,7 +5,7 @@
   stable ids, working order) -- the oracle performs the kernels' operation
   sequence with the same fused multiply-adds.
 * Within FP32 tolerance of the FP64 oracle (reference formulas in double)
-  after 1 and 10 steps, the spec accuracy check.
+  after 1 and 10 steps, the accuracy check of the FP32 solver.
 """
 
 import numpy as np
