@@ -23,12 +23,16 @@ def run_alone(pbf, per, steps):
     return out
 
 
-@pytest.mark.parametrize("steps", [1, 6])
-def test_batch_equals_each_scene_alone(pbf, scenes, steps):
+@pytest.mark.parametrize("steps,lanes", [(1, 0), (6, 1), (6, 4)])
+def test_batch_equals_each_scene_alone(pbf, scenes, steps, lanes):
+    """Every scene of a batch steps bit for bit as it does alone (each scene
+    alone walks split over 4 lanes, the default below 32,768 particles; the
+    batch of 28,716 particles with the default, 1 or 4 lanes)."""
     sc, prm, pos, vel, per = scenes.batched_scenes(n_scenes=12, n_min=512, n_max=8192, seed=11)
     b = pbf.PBFSolver()
     b.initialize_batch(sc, prm)
     assert b.scene_count() == 12
+    b.set_walk_lanes(lanes)
     b.set_particles(pos, vel)
     b.run(steps)
     bp, bv = b.copy_positions_to_host(), b.copy_velocities_to_host()
