@@ -382,8 +382,7 @@ class PBFSolver:
                      "confine")
 
     def autotune(self, frames_per_trial: int = 2) -> dict:
-        """pbf_autotune: choose the neighbour kernels' block sizes (returned)
-        and the lanes per particle of the walks (walk_lanes())."""
+        """pbf_autotune: choose the neighbour kernels' block sizes; returns them."""
         self._check(self._L.pbf_autotune(self._h, int(frames_per_trial)))
         return self.block_sizes()
 

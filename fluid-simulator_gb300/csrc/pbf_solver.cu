@@ -199,7 +199,7 @@ struct pbf_solver {
 
     // Threads per block of the tuned kernels (0 = the default 256).
     int tuned[kTunedCount] = {};
-    int tuned_lanes = 0;  // lanes per particle of the walks chosen by autotune; 0 = default
+    int tuned_lanes = 0;  // lanes per particle of the walks set by pbf_set_walk_lanes; 0 = default
 
     // Compact neighbour lists (list_cap > 0): every rebuild counts the
     // neighbours, scans the counts into nb_off and writes each particle's
@@ -553,12 +553,10 @@ struct pbf_solver {
         std::vector<int> launches(kStageCount);
         int saved[kTunedCount];
         std::copy(tuned, tuned + kTunedCount, saved);
-        const int saved_lanes = tuned_lanes;
         try {
             tune_all(frames_per_trial, ms, launches, sx.as<float4>(), sv.as<float4>());
         } catch (...) {
             std::copy(saved, saved + kTunedCount, tuned);
-            tuned_lanes = saved_lanes;
             clear_graphs();
             set_particles(sx.as<float4>(), sv.as<float4>(), n, true);
             throw;
@@ -569,6 +567,17 @@ struct pbf_solver {
 
     // Every trial frame starts from the saved state (x0, v0), so the sizes are
     // compared on the same work.
+    // Frames of a trial before the timed ones: set_particles alternates the
+    // buffers, so the first two frames capture and first launch the two
+    // graphs a trial uses; they are not timed.
+    void warm_trial(std::vector<float>& ms, std::vector<int>& launches, const float4* x0,
+                    const float4* v0) {
+        for (int f = 0; f < 2; ++f) {
+            set_particles(x0, v0, n, true);
+            profile_frame(ms.data(), launches.data());
+        }
+    }
+
     void tune_all(int frames_per_trial, std::vector<float>& ms, std::vector<int>& launches,
                   const float4* x0, const float4* v0) {
         static const int stage_of[kTunedCount] = {kStSearchLambda, kStDeltaApply, kStSearch,
@@ -580,6 +589,7 @@ struct pbf_solver {
             for (int b : sizes) {
                 tuned[k] = b;
                 clear_graphs();
+                warm_trial(ms, launches, x0, v0);
                 float t = -1.0f;
                 for (int f = 0; f < frames_per_trial; ++f) {
                     set_particles(x0, v0, n, true);
@@ -595,31 +605,10 @@ struct pbf_solver {
             }
             tuned[k] = best;
         }
-        // Lanes per particle of the two list-writing walks, timed together.
-        if (list_cap > 0) return;
-        int best = walk_lanes();
-        float best_ms = -1.0f;
-        for (int L : {1, 2, 4}) {
-            if (max_nb < L) continue;
-            tuned_lanes = L;
-            clear_graphs();
-            float t = -1.0f;
-            for (int f = 0; f < frames_per_trial; ++f) {
-                set_particles(x0, v0, n, true);
-                profile_frame(ms.data(), launches.data());
-                const float v = ms[kStSearchLambda] + ms[kStSearch];
-                t = t < 0.0f ? v : std::min(t, v);
-            }
-            if (best_ms < 0.0f || t < best_ms) {
-                best_ms = t;
-                best = L;
-            }
-        }
-        tuned_lanes = best;
     }
 
-    // Lanes per particle of the list-writing walks: the tuned value, else
-    // the default for the scene size; 1 with compact lists.
+    // Lanes per particle of the list-writing walks: the value set, else the
+    // default for the scene size; 1 with compact lists.
     int walk_lanes() const {
         if (list_cap > 0) return 1;
         const int L = tuned_lanes > 0 ? tuned_lanes : default_walk_lanes(n, max_nb);

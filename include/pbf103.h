@@ -158,17 +158,15 @@ int pbf_batch_scene_count(const pbf_solver* s);
 /* Block-size autotuner (no counterpart in the reference): for the six
  * neighbour kernels (walk + lambda, delta p, final walk, XSPH, vorticity,
  * confinement), times each at 128, 256 and 512 threads per block in profiled
- * frames (`frames_per_trial` per size) and keeps the fastest; then, with
- * slot-major lists, times the two list-writing walks with 1, 2 and 4 lanes
- * per particle (each particle's stencil rows split over the lanes) and keeps
- * the fastest.  Results do not change (neither choice changes the lists or
- * any arithmetic); the particle state is restored, so tuning does not advance
- * the simulation.  Needs particles set. */
+ * frames (`frames_per_trial` per size, after two untimed frames) and keeps
+ * the fastest.  Results do not change (block size changes no arithmetic);
+ * the particle state is restored, so tuning does not advance the simulation.
+ * Needs particles set. */
 pbf_status pbf_autotune(pbf_solver* s, int frames_per_trial);
 /* The block sizes in use, in the order above (count <= 6 entries). */
 pbf_status pbf_block_sizes(const pbf_solver* s, int* sizes, int count);
-/* Lanes per particle of the list-writing walks in use: the tuned or set
- * value, else 4 below 32,768 particles and 1 from there on (always 1 with
+/* Lanes per particle of the list-writing walks in use: the value set by
+ * pbf_set_walk_lanes, else 4 below 32,768 particles and 1 from there on (always 1 with
  * compact lists; at most max_neighbors). */
 pbf_status pbf_walk_lanes(const pbf_solver* s, int* lanes);
 /* Sets the lanes per particle of the walks: 1, 2 or 4, or 0 for the default
