@@ -170,7 +170,9 @@ pbf_status pbf_block_sizes(const pbf_solver* s, int* sizes, int count);
  * compact lists; at most max_neighbors). */
 pbf_status pbf_walk_lanes(const pbf_solver* s, int* lanes);
 /* Sets the lanes per particle of the walks: 1, 2 or 4, or 0 for the default
- * by scene size.  Results do not change. */
+ * by scene size.  Results do not change.  The split pays when one small scene
+ * leaves the GPU idle; many small solvers running at once on separate streams
+ * step faster with 1 (256 scenes: 11.3 against 18.4 ms per step). */
 pbf_status pbf_set_walk_lanes(pbf_solver* s, int lanes);
 
 /* ---- reverse-mode derivative (no counterpart in the reference) ---------
