@@ -536,7 +536,7 @@ struct pbf_solver {
     }
 
     // Block-size autotuner: for each tuned kernel, time its stage in profiled
-    // frames at 128, 256 and 512 threads per block and keep the fastest
+    // frames at 64, 128, 256 and 512 threads per block and keep the fastest
     // (coordinate descent, one kernel at a time; the other kernels keep their
     // current sizes).  Block size changes no arithmetic, so results stay bit
     // for bit the same.  The particle state is saved before and restored
@@ -582,7 +582,7 @@ struct pbf_solver {
                   const float4* x0, const float4* v0) {
         static const int stage_of[kTunedCount] = {kStSearchLambda, kStDeltaApply, kStSearch,
                                                   kStXsph, kStVorticity, kStConfine};
-        static const int sizes[3] = {128, 256, 512};
+        static const int sizes[4] = {64, 128, 256, 512};
         for (int k = 0; k < kTunedCount; ++k) {
             int best = tuned[k] > 0 ? tuned[k] : kBlock;
             float best_ms = -1.0f;

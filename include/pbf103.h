@@ -157,7 +157,7 @@ int pbf_batch_scene_count(const pbf_solver* s);
 
 /* Block-size autotuner (no counterpart in the reference): for the six
  * neighbour kernels (walk + lambda, delta p, final walk, XSPH, vorticity,
- * confinement), times each at 128, 256 and 512 threads per block in profiled
+ * confinement), times each at 64, 128, 256 and 512 threads per block in profiled
  * frames (`frames_per_trial` per size, after two untimed frames) and keeps
  * the fastest.  Results do not change (block size changes no arithmetic);
  * the particle state is restored, so tuning does not advance the simulation.
