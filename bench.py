@@ -20,8 +20,11 @@ e2e       the same metric through the public API with host buffers: every step
           pinned host memory.
 roofline  dominant kernel of the step, timed live with CUDA events captured
           in the frame graph, against the measured HBM copy bandwidth.
+vs_baseline  value over the reference's own CUDA kernels on the same GPU,
+          same workload and the same frames (the metric's comparison).
 --impl reference  the CPU restatement of the reference step (the reference
-          has no CPU implementation) on all host cores, bounded sample.
+          has no CPU implementation) on all host cores, over the same warm-up
+          and timed steps when they fit PBF_REF_SECONDS, else a bounded sample.
 """
 
 from __future__ import annotations
@@ -71,30 +74,43 @@ STAGE_BYTES = {
 }
 
 
-# DRAM bytes per launch of the dominant kernel (k_search<1>: walk + lambda)
-# from one ncu capture of the 1M dam break at frame 150, the state the timed
-# region averages over (profiles/k_search_dam_break_1m_frame150.md).
-TRAFFIC_BYTES = {"search_lambda": 103.668736e6 + 165.316864e6}
-# Warp instructions per launch of the same capture (smsp__inst_executed.sum):
-# the walk is issue-bound, so its issue rate is the roofline that binds it.
-INST_PER_LAUNCH = {"search_lambda": 245930457.0}
+# ncu captures of the dominant kernel (k_search<1>: walk + lambda) on the
+# 1M dam break, one launch each, keyed by the frame they were taken at:
+# DRAM bytes read + written (dram__bytes_read.sum + dram__bytes_write.sum)
+# and warp instructions (smsp__inst_executed.sum).  A timed window is matched
+# with the capture nearest its middle frame; the line names that frame.
+CAPTURES = {
+    "search_lambda": {
+        150: {"dram_bytes": 103.668736e6 + 165.316864e6, "inst": 245930457.0},
+    },
+}
 SMS, ISSUE_PER_SM_CLK = 152, 4
 
 
-def issue_roofline(kernel, ms_per_launch, clocks, scene):
+def capture_for(kernel, scene, mid_frame):
+    """The capture of `kernel` nearest frame `mid_frame` of the 1M dam break."""
+    caps = CAPTURES.get(kernel) if scene == "dam_break_1m" else None
+    if not caps:
+        return None, None
+    frame = min(caps, key=lambda f: abs(f - mid_frame))
+    return frame, caps[frame]
+
+
+def issue_roofline(kernel, ms_per_launch, clocks, scene, mid_frame):
     """Warp instructions per second of the dominant kernel against the SMs'
-    issue peak (4 per SM per clock at the SM clock sampled while timing)."""
-    inst = INST_PER_LAUNCH.get(kernel) if scene == "dam_break_1m" else None
+    issue peak (4 per SM per clock at the SM clock sampled while timing),
+    with the instruction count of the capture nearest the timed window."""
+    frame, cap = capture_for(kernel, scene, mid_frame)
     mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
-    if not inst or not mhz:
+    if not cap or not mhz:
         return None
-    achieved = inst / (ms_per_launch / 1000.0) / 1e9
+    achieved = cap["inst"] / (ms_per_launch / 1000.0) / 1e9
     peak = SMS * ISSUE_PER_SM_CLK * mhz * 1e6 / 1e9
     return {"bound": "issue", "kernel": kernel, "achieved": achieved, "peak": peak,
             "unit": "G warp-instructions/s", "frac": achieved / peak,
-            "inst_per_launch": inst,
-            "source": "smsp__inst_executed.sum of one ncu capture at frame 150 "
-                      "(profiles/k_search_dam_break_1m_frame150.md)"}
+            "inst_per_launch": cap["inst"], "captured_at_frame": frame,
+            "window_mid_frame": mid_frame,
+            "source": "smsp__inst_executed.sum of one ncu capture (--clock-control none)"}
 
 
 def load_pkg():
@@ -228,8 +244,14 @@ def pinned_like(a: np.ndarray):
         return None, np.ascontiguousarray(a).copy()
 
 
-def cpu_baseline(scene, seconds_budget: float = 20.0, threads: int = 0):
-    """FP32 restatement of the reference step (oracle, OpenMP) on the host cores."""
+def cpu_baseline(scene, seconds_budget: float = 20.0, threads: int = 0, warmup: int = 1,
+                 steps: int = 0):
+    """FP32 restatement of the reference step (oracle, OpenMP) on the host cores.
+
+    `warmup` untimed steps, then `steps` timed steps (the GPU arm's window);
+    when those would take longer than `seconds_budget` (estimated from the
+    first warm-up step), or when steps == 0, as many steps as fit the budget.
+    The line reports the steps actually timed."""
     from oracle import oracle as O
     pos, vel, mn, mx, prm, _ = scene
     threads = threads or os.cpu_count() or 1
@@ -237,26 +259,47 @@ def cpu_baseline(scene, seconds_budget: float = 20.0, threads: int = 0):
     o.initialize(len(pos), mn, mx, prm.as_dict())
     o.set_particles(pos, vel)
     t0 = time.perf_counter()
-    st = o.step()  # warm-up step (first touch of the lists)
-    warm = time.perf_counter() - t0
+    st = o.step()  # first warm-up step (first touch of the lists)
+    first = time.perf_counter() - t0
     if st != 0:
         raise RuntimeError("oracle step failed: %d" % st)
-    steps = max(1, int(seconds_budget / max(warm, 1e-3)))
+    for _ in range(max(warmup, 1) - 1):
+        st = o.step()
+        if st != 0:
+            raise RuntimeError("oracle step failed: %d" % st)
+    fit = max(1, int(seconds_budget / max(first, 1e-3)))
+    timed = min(steps, fit) if steps > 0 else fit
     t0 = time.perf_counter()
-    for _ in range(steps):
+    for _ in range(timed):
         st = o.step()
         if st != 0:
             raise RuntimeError("oracle step failed: %d" % st)
     dt = time.perf_counter() - t0
-    return {"value": len(pos) * steps / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": "%d steps of the full %d-particle workload after 1 warm-up step "
-                      "(FP32 C++/OpenMP restatement, %.1f s)" % (steps, len(pos), dt)}
+    whole = steps > 0 and timed == steps
+    return {"value": len(pos) * timed / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "steps": timed, "warmup": max(warmup, 1),
+            "sample": "steps %d..%d of the full %d-particle workload (%s; FP32 C++/OpenMP "
+                      "restatement on %d threads, %.1f s)"
+                      % (max(warmup, 1), max(warmup, 1) + timed, len(pos),
+                         "the same window as the GPU arm" if whole else
+                         "a bounded sample of %d steps" % timed, threads, dt)}
+
+
+def density_of(positions, scene):
+    """FP64 density error of a final state (oracle.density_stats): the same
+    measure for this library's and the reference's positions."""
+    from oracle import oracle as O
+    _, _, mn, mx, prm, _ = scene
+    return O.density_stats(positions, mn, mx, prm.smoothingRadius, prm.particleMass,
+                           prm.restDensity)
 
 
 def reference_cuda(scene, steps: int, warmup: int, max_neighbors: int = 256):
     """The reference's own kernels (compiled from its sources, Release, sm_103a)
     driven with PBFSolver's host sequence, timed like its benchmark: steady
-    clock around each step() (benchmark/pbf_benchmark.cu:121-137)."""
+    clock around each step() (benchmark/pbf_benchmark.cu:121-137).  Steps
+    warmup .. warmup + steps of the run, the window this library is timed on;
+    the density error of the final state is measured as for this library."""
     from oracle import oracle as O
     from oracle import build_ref
     if not build_ref.available():
@@ -274,12 +317,70 @@ def reference_cuda(scene, steps: int, warmup: int, max_neighbors: int = 256):
     if st != 0:
         return {"unavailable": "reference step failed with status %d" % st}
     ms = r.time_steps(steps)
+    final = r.positions()
     r.close()
     return {"value": len(pos) * steps / (ms / 1000.0), "unit": UNIT, "ms_per_step": ms / steps,
             "steps": steps, "warmup": warmup, "max_neighbors": max_neighbors,
+            "density_error": density_of(final, scene),
             "method": "reference kernels compiled from its sources (-O3 -DNDEBUG, sm_103a), "
                       "PBFSolver host sequence and synchronisation, steady_clock around each "
                       "step()"}
+
+
+def configured_parameters(pkg, scene, steps: int = 100):
+    """The 1M lattice with the configuration's literal step parameters (one
+    step of dt = 1/60, s_corr k = 0.1, XSPH c = 0.01, vorticity 1e-4): how
+    far the reference's kernels and this library get before a step fails
+    (neighbour overflow) and the fastest particle when they stop."""
+    import dataclasses
+    from oracle import oracle as O
+    from oracle import build_ref
+    pos, vel, mn, mx, prm, _ = scene
+    cfg = dataclasses.replace(prm, dt=1.0 / 60.0, scorrK=0.1, xsphViscosity=0.01,
+                              vorticityStrength=1e-4)
+    out = {"params": {"dt": cfg.dt, "scorrK": cfg.scorrK, "xsphViscosity": cfg.xsphViscosity,
+                      "vorticityStrength": cfg.vorticityStrength}, "max_steps": steps}
+
+    def speed(v):
+        return float(np.sqrt((v[:, :3].astype(np.float64) ** 2).sum(1).max()))
+
+    if build_ref.available():
+        r = O.RefCudaSolver()
+        r.initialize(len(pos), mn, mx, cfg.as_dict())
+        r.set_colliders(np.zeros((0, 4), np.float32), np.zeros((0, 6), np.float32),
+                        np.zeros((0, 6), np.float32))
+        r.set_particles(pos, vel)
+        done, st, vmax = 0, 0, 0.0
+        while done < steps:
+            st = r.step()
+            if st != 0:
+                break
+            done += 1
+            if done in (1, 2, 5, 10, 20, 50, 100):
+                vmax = speed(r.velocities())
+        out["reference_cuda"] = {
+            "steps_completed": done,
+            "status": {0: "ok", 1: "error", 2: "overflow_error (neighbour capacity 256)",
+                       3: "not converged"}.get(st, str(st)),
+            "max_speed_before_stop": vmax}
+        r.close()
+    s = pkg.PBFSolver()
+    s.initialize(len(pos), mn, mx, cfg)
+    s.set_particles(pos, vel)
+    done, err, vmax = 0, None, 0.0
+    while done < steps:
+        try:
+            s.step()
+        except pkg.PBFError as e:
+            err = type(e).__name__ + ": " + str(e)[:120]
+            break
+        done += 1
+        if done in (1, 2, 5, 10, 20, 50, 100):
+            vmax = speed(s.copy_velocities_to_host())
+    s.close()
+    out["this_library"] = {"steps_completed": done, "status": err or "ok",
+                           "max_speed_before_stop": vmax}
+    return out
 
 
 def reference_scene(pkg, scenes, frames: int = 60, reps: int = 5, warmup: int = 10):
@@ -636,25 +737,29 @@ def adjoint_reference_scene(pkg, scenes, frames: int = 10, every: int = 5):
 
 
 def run_reference(args):
+    """The reference arm: the reference ships no CPU implementation of the
+    step, so its CPU restatement (oracle/pbf_oracle.cpp, FP32, OpenMP on all
+    host cores) runs the GPU arm's workload and window: `--warmup` untimed
+    steps, then `--steps` timed steps, bounded to PBF_REF_SECONDS (default
+    240) of timed CPU work."""
     rank, world, local = dist_env()
     if rank != 0:
         return 0
     pkg = load_pkg()
     scenes = importlib.import_module("fluid_simulator_gb300.scenes")
     scene = scenes.dam_break_1m()
-    budget = float(os.environ.get("PBF_REF_SECONDS", "60"))
-    cb = cpu_baseline(scene, seconds_budget=budget)
+    budget = float(os.environ.get("PBF_REF_SECONDS", "240"))
+    cb = cpu_baseline(scene, seconds_budget=budget, warmup=args.warmup, steps=args.steps)
     n = len(scene[0])
-    steps_done = int(round(cb["value"] * budget / n)) if cb["value"] else 0
     line = {
         "impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT,
-        "n_gpus": world, "steps": steps_done, "warmup": 1,
+        "n_gpus": world, "steps": cb["steps"], "warmup": cb["warmup"],
         "ms_per_step": 1000.0 * n / cb["value"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic: seeded 128x128x64 dam-break lattice",
         "config": {"workload": WORKLOAD, "particles": n, "iterations": 4,
                    "implementation": "CPU restatement of the reference step (the reference "
-                                     "ships CUDA only); bounded sample"},
+                                     "ships CUDA only)"},
         "cpu_baseline": cb,
         "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
@@ -678,6 +783,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default 256-thread blocks")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-configured", action="store_true",
+                    help="skip the run with the configuration's literal step parameters")
     ap.add_argument("--no-reference-scene", action="store_true",
                     help="skip the reference's own 262,144-particle benchmark scene")
     ap.add_argument("--adjoint-steps", type=int, default=60)
@@ -711,7 +818,8 @@ def main():
     s.set_particles(pos, vel)
     s.run(args.warmup)
     tuned = s.autotune(2) if not args.no_autotune else s.block_sizes()
-    s.run(1)
+    s.run(1)  # re-instantiates the frame graphs after tuning
+    first_timed = args.warmup + 1  # frames before the timed window
     kernels = s.kernels_per_frame()
 
     # ---- device-timed value -------------------------------------------------
@@ -724,6 +832,7 @@ def main():
     barrier(dist)
     ms_max = allreduce_max(dist, ms)
     value = n * args.steps * world / (ms_max / 1000.0)
+    final_positions = s.copy_positions_to_host() if rank == 0 and world == 1 else None
 
     # ---- dominant kernel, timed live in the frame graph ---------------------
     prof = {}
@@ -778,6 +887,8 @@ def main():
     e2e_value = n * args.e2e_steps * world / e2e_s
 
     density = s.density_error()
+    mid_frame = first_timed + args.steps // 2
+    cap_frame, cap = capture_for(dom, args.scene, mid_frame)
 
     line = None
     if rank == 0:
@@ -806,23 +917,40 @@ def main():
             "kernels_per_step": kernels,
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
                          "unit": "GB/s", "frac": achieved / hbm,
-                         "traffic": TRAFFIC_BYTES.get(dom) if args.scene == "dam_break_1m"
-                         else None,
+                         "traffic": cap["dram_bytes"] if cap else None,
+                         "traffic_captured_at_frame": cap_frame,
+                         "window_frames": [first_timed, first_timed + args.steps],
                          "peak_source": peak_kind,
                          "algorithmic_bytes_per_launch": dom_bytes,
                          "ms_per_launch": stages[dom]["ms_per_launch"]},
             "issue_roofline": issue_roofline(dom, stages[dom]["ms_per_launch"], clocks,
-                                             args.scene),
+                                             args.scene, mid_frame),
             "step_roofline": {"bytes_per_particle_step": balg, "achieved": step_achieved,
                               "peak": hbm, "unit": "GB/s", "frac": step_achieved / hbm},
             "stages": stages,
-            "density_error": {"mean": density[0], "max": density[1]},
+            "density_error": {"mean": density[0], "max": density[1],
+                              "lists": "this library's own lists after the e2e steps"},
         }
+        if final_positions is not None:
+            line["density_error_fp64"] = dict(
+                density_of(final_positions, scene),
+                state="frame %d (end of the timed window), FP64 over all pairs within h"
+                      % (first_timed + args.steps))
         if world == 1 and not args.no_reference_cuda:
-            line["reference_cuda"] = reference_cuda(scene, args.steps, args.warmup,
+            line["reference_cuda"] = reference_cuda(scene, args.steps, first_timed,
                                                     args.max_neighbors)
             if "value" in line["reference_cuda"]:
-                line["speedup_vs_reference_cuda"] = value / line["reference_cuda"]["value"]
+                ratio = value / line["reference_cuda"]["value"]
+                line["speedup_vs_reference_cuda"] = ratio
+                # The metric is quoted against the reference's CUDA solver: the
+                # same workload and window on the same GPU, measured here.
+                line["vs_baseline"] = ratio
+                line["vs_baseline_basis"] = (
+                    "value / the reference's own CUDA kernels' particle-steps/s, same "
+                    "workload, same GPU, same frames %d..%d"
+                    % (first_timed, first_timed + args.steps))
+        if world == 1 and not args.no_configured:
+            line["configured_parameters"] = configured_parameters(pkg, scene)
         if world == 1 and not args.no_reference_scene:
             line["reference_scene"] = reference_scene(pkg, scenes)
         if world == 1 and not args.no_batched:
@@ -834,7 +962,8 @@ def main():
             line["adjoint_reference_scene"] = adjoint_reference_scene(pkg, scenes)
         if not args.no_cpu_baseline and world == 1:
             budget = float(os.environ.get("PBF_CPU_SECONDS", "20"))
-            line["cpu_baseline"] = cpu_baseline(scene, seconds_budget=budget)
+            line["cpu_baseline"] = cpu_baseline(scene, seconds_budget=budget,
+                                                warmup=first_timed, steps=args.steps)
         print(json.dumps(line), flush=True)
     s.close()
     if dist is not None:

@@ -214,7 +214,7 @@ k_gather_first(const uint32_t* __restrict__ perm, const float4* __restrict__ xs_
 // ---------------------------------------------------------------------------
 // Neighbour walk.  Order of the list = z -> y -> x over the clamped cells,
 // ascending sorted index inside a cell, self skipped, accept d2 <= h2
-// (src/pbf/neighbors.cu:319-358).  With LAMBDA the constraint terms of
+// (src/pbf/neighbors.cu:52-86).  With LAMBDA the constraint terms of
 // computeLambda are accumulated in that same list order.
 // ---------------------------------------------------------------------------
 struct LambdaAcc {
@@ -291,7 +291,7 @@ __device__ __forceinline__ int walk(const StepConst& c, int i, float4 pi,
     int count = 0;
     // Rows z -> y; inside a row the cells x0..x1 are consecutive keys, so the
     // candidates of the row are one index range walked in ascending order --
-    // exactly the reference's z -> y -> x cell walk (neighbors.cu:319-354).
+    // exactly the reference's z -> y -> x cell walk (neighbors.cu:52-86).
     // Each range is scanned in 32-candidate chunks starting at an even index:
     // pairs of candidates are tested with FP32x2 arithmetic on the component
     // arrays (8-byte loads), the results go into a hit mask without branches,

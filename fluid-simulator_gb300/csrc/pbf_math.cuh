@@ -71,7 +71,7 @@ __device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
 __device__ __forceinline__ f32x2 splat2(float a) { return pack2(a, a); }
 
 // Squared length, rounded as the reference's compiled findNeighbors rounds
-// dx*dx + dy*dy + dz*dz (src/pbf/neighbors.cu:338-342): nvcc contracts it to
+// dx*dx + dy*dy + dz*dz (src/pbf/neighbors.cu:73-74): nvcc contracts it to
 // fma(dz, dz, fma(dy, dy, dx*dx)).  Neighbour lists can only match the
 // reference bit for bit with this exact rounding.
 __device__ __forceinline__ float dist2(float dx, float dy, float dz) {

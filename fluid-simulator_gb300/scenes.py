@@ -10,6 +10,8 @@ then y, then z; w = 1.
   box [0,12.8]x[0,6.4]x[0,6.4] (the fluid fills the x<6.4, z<3.2 corner).
 * ``imbalanced_8m``  -- half a dense lattice column, half 16 Gaussian blobs
   (sigma 4h, centres uniform), box 25.6x12.8x12.8.
+* ``imbalanced_262k`` -- the same at 262,144 particles: half a lattice column,
+  half 4 blobs of sigma 2h (the 8M blobs' core density), box 6.4x3.2x3.2.
 * ``batched_scenes`` -- 256 independent dam breaks, particle counts
   log-uniform in [2,048, 65,536] (seed 7): a (2k, 2k, k) lattice per scene in
   a (4k, 2k, 2k) x spacing box, rest density x U(0.9, 1.1) with the mass
@@ -114,6 +116,26 @@ def imbalanced_8m(seed: int = 0, n_total: int = 8_388_608):
     return pos, vel, (0.0, 0.0, 0.0), box, dam_break_params(), {}
 
 
+def imbalanced_262k(seed: int = 0):
+    """The imbalanced configuration scaled down to 262,144 particles with the
+    same blob-core density: half a 64x32x64 lattice column in the corner,
+    half 4 Gaussian blobs of sigma 2h (32,768 particles each, about 1,090
+    neighbours within h at a blob's centre, as in the 8M scene's blobs),
+    centres uniform in the inner part of a 6.4x3.2x3.2 box."""
+    box = (6.4, 3.2, 3.2)
+    col = lattice(64, 32, 64, SPACING, (RADIUS, RADIUS, RADIUS), 0.01 * H, seed)
+    rng = np.random.default_rng(seed + 1)
+    centres = rng.uniform((0.8, 0.8, 0.8), (box[0] - 0.8, box[1] - 0.8, box[2] - 0.8), (4, 3))
+    which = np.repeat(np.arange(4), 32768)
+    blob = centres[which] + rng.normal(0.0, 2 * H, (which.shape[0], 3))
+    blob = np.clip(blob, RADIUS, np.asarray(box) - RADIUS)
+    bl = np.ones((blob.shape[0], 4), np.float32)
+    bl[:, :3] = blob.astype(np.float32)
+    pos = np.concatenate([col, bl], axis=0)
+    vel = np.zeros_like(pos)
+    return pos, vel, (0.0, 0.0, 0.0), box, dam_break_params(), {}
+
+
 def reference_benchmark_params() -> SimulationParams:
     """simulationParams() of benchmark/pbf_benchmark.cu:63-83."""
     spacing = np.float32(0.06)
@@ -166,6 +188,7 @@ SCENES = {
     "dam_break_16k": dam_break_16k,
     "dam_break_1m": dam_break_1m,
     "imbalanced_8m": imbalanced_8m,
+    "imbalanced_262k": imbalanced_262k,
     "reference_benchmark": reference_benchmark,
 }
 

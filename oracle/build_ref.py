@@ -9,7 +9,10 @@ driver in oracle/ref_driver.cu loads it there.  Nothing is copied: the
 sources are read where they lie.
 
 build_if_possible() is a no-op when the reference tree is absent (the GPU machine
-uses the fatbins built here).
+uses the fatbins built here).  The reference tree is taken from the
+PBF_REFERENCE_DIR environment variable, or from `--reference DIR` when this
+recipe runs as a script; without either, the recipe looks in the one place
+the reference is checked out for this project's checker builds.
 """
 
 from __future__ import annotations
@@ -21,7 +24,7 @@ import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REFERENCE = "/root/reference"
+REFERENCE = os.environ.get("PBF_REFERENCE_DIR") or "/root/reference"
 UNITS = ["integration", "neighbors", "pbf_solver_kernels", "collision_kernels", "spatial_grid"]
 FLAGS = ["-fatbin", "-std=c++20", "-O3", "-DNDEBUG", "-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -79,5 +82,11 @@ def compile_benchmark_on_shim(lib_path: str, include_dir: str, out_path: str) ->
 
 
 if __name__ == "__main__":
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", default=None, help="reference source tree")
+    a = ap.parse_args()
+    if a.reference:
+        REFERENCE = a.reference
     build(force=True)
     print("\n".join(fatbin_path(u) for u in UNITS))

@@ -132,6 +132,10 @@ def lib():
         L.orc_solver_copy_working.restype = C.c_int
         L.orc_solver_density_error.argtypes = [_vp, C.POINTER(C.c_double),
                                                C.POINTER(C.c_double)]
+        L.orc_density_stats.argtypes = [_vp, C.c_size_t, F3, F3, C.c_float, C.c_float,
+                                        C.c_float, C.POINTER(C.c_double),
+                                        C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.orc_density_stats.restype = C.c_int
     return _lib
 
 
@@ -253,6 +257,18 @@ def confinement(pos, nb, cnt, cap, omega, vin, stride, h, dt, eps):
     lib().orc_confinement(_p(pos), _p(nb), _p(cnt), cap, _p(as_f4(omega)), _p(as_f4(vin)),
                           _p(out), pos.shape[0], stride, h, dt, eps)
     return out
+
+
+def density_stats(pos, mn, mx, h, mass, rho0):
+    """|rho/rho0 - 1| of a set of positions, FP64 over all pairs within h:
+    {"mean", "max", "frac_above_10pct"} -- the same yardstick for any solver."""
+    pos = as_f4(pos)
+    m, x, f = C.c_double(), C.c_double(), C.c_double()
+    st = lib().orc_density_stats(_p(pos), pos.shape[0], f3(mn), f3(mx), h, mass, rho0,
+                                 C.byref(m), C.byref(x), C.byref(f))
+    if st != ORC_OK:
+        raise ValueError("orc_density_stats failed: %d" % st)
+    return {"mean": m.value, "max": x.value, "frac_above_10pct": f.value}
 
 
 # ---- collisions ---------------------------------------------------------------

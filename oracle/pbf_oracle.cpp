@@ -65,7 +65,7 @@ struct F32 {
         c_spiky = -45.0f / kPiF / hh / hh / hh / hh;
     }
     // Squared length rounded as the reference's compiled findNeighbors rounds
-    // dx*dx + dy*dy + dz*dz (src/pbf/neighbors.cu:338-342): fma(dz, dz,
+    // dx*dx + dy*dy + dz*dz (src/pbf/neighbors.cu:73-74): fma(dz, dz,
     // fma(dy, dy, dx*dx)).
     static T dist2(T dx, T dy, T dz) { return std::fma(dz, dz, std::fma(dy, dy, dx * dx)); }
     static T len(T x, T y, T z) { return std::sqrt(dist2(x, y, z)); }
@@ -258,7 +258,7 @@ void stable_sort_keys(const uint32_t* keys, size_t n, size_t cells, uint32_t* so
     }
 }
 
-// findNeighbors' neighbourhood radius in cells (src/pbf/neighbors.cu:307-317):
+// findNeighbors' neighbourhood radius in cells (src/pbf/neighbors.cu:39-50):
 // ceil in double, then the [first, last] bounds clamped to the grid.
 inline void search_bounds(const Grid& g, double radius, const int c[3], int first[3],
                           int last[3]) {
@@ -272,7 +272,7 @@ inline void search_bounds(const Grid& g, double radius, const int c[3], int firs
 template <class T> inline T vsub(T a, T b) { return a - b; }
 
 // One particle's cell walk: z -> y -> x over clamped cells, ranges in sorted
-// order, self skipped, accept d2 <= h2 (src/pbf/neighbors.cu:319-358).
+// order, self skipped, accept d2 <= h2 (src/pbf/neighbors.cu:52-86).
 // Visitor receives every accepted neighbour index in list order.
 template <class P, class Pos, class Visit>
 int walk_neighbors(const P& m, const Grid& g, double radius, const Pos* sp, size_t i,
@@ -1182,6 +1182,70 @@ int orc_solver_copy_working(const orc_solver* s, orc_float4* pos, uint32_t* ids,
 }
 int orc_solver_density_error(const orc_solver* s, double* mean, double* mx) {
     return s->impl->density_error(mean, mx);
+}
+
+// The density that computeLambda forms (src/pbf/pbf_solver_kernels.cu:50-75),
+// in double and over all pairs within h found through cells of size h: a
+// yardstick for comparing two solvers' final states, independent of either
+// solver's own lists.
+int orc_density_stats(const orc_float4* pos, size_t n, orc_float3 mn, orc_float3 mx, float h,
+                      float mass, float rho0, double* meanErr, double* maxErr,
+                      double* fracAbove10) {
+    int d[3];
+    const int st = grid_dims(mn, mx, h, d);
+    if (st != ORC_OK) return st;
+    const size_t cells = size_t(d[0]) * size_t(d[1]) * size_t(d[2]);
+    std::vector<uint32_t> key(n), start(cells + 1, 0), order(n);
+    const double inv = 1.0 / double(h);
+    auto cell = [&](double p, float lo, int dim) {
+        const double c = std::floor((p - double(lo)) * inv);
+        return c < 0.0 ? 0 : (c > double(dim - 1) ? dim - 1 : int(c));
+    };
+    for (size_t i = 0; i < n; ++i) {
+        const int cx = cell(pos[i].x, mn.x, d[0]), cy = cell(pos[i].y, mn.y, d[1]),
+                  cz = cell(pos[i].z, mn.z, d[2]);
+        key[i] = uint32_t(cx + size_t(d[0]) * (cy + size_t(d[1]) * cz));
+        ++start[key[i] + 1];
+    }
+    for (size_t c = 0; c < cells; ++c) start[c + 1] += start[c];
+    {
+        std::vector<uint32_t> fill(start.begin(), start.end() - 1);
+        for (size_t i = 0; i < n; ++i) order[fill[key[i]]++] = uint32_t(i);
+    }
+    const double hh = double(h), h2 = hh * hh;
+    const double norm = 315.0 / (64.0 * kPiD * hh * hh * hh * hh * hh * hh * hh * hh * hh);
+    double sum = 0.0, mxe = 0.0;
+    long long above = 0;
+#pragma omp parallel for schedule(dynamic, 4096) reduction(+ : sum, above) reduction(max : mxe)
+    for (long long ii = 0; ii < (long long)n; ++ii) {
+        const size_t i = size_t(ii);
+        const int cx = cell(pos[i].x, mn.x, d[0]), cy = cell(pos[i].y, mn.y, d[1]),
+                  cz = cell(pos[i].z, mn.z, d[2]);
+        double w = 0.0;
+        for (int z = std::max(0, cz - 1); z <= std::min(d[2] - 1, cz + 1); ++z)
+            for (int y = std::max(0, cy - 1); y <= std::min(d[1] - 1, cy + 1); ++y)
+                for (int x = std::max(0, cx - 1); x <= std::min(d[0] - 1, cx + 1); ++x) {
+                    const size_t c = size_t(x) + size_t(d[0]) * (size_t(y) + size_t(d[1]) * z);
+                    for (uint32_t k = start[c]; k < start[c + 1]; ++k) {
+                        const orc_float4 q = pos[order[k]];
+                        const double dx = double(pos[i].x) - q.x, dy = double(pos[i].y) - q.y,
+                                     dz = double(pos[i].z) - q.z;
+                        const double r2 = dx * dx + dy * dy + dz * dz;
+                        if (r2 < h2) {
+                            const double t = h2 - r2;
+                            w += norm * t * t * t;
+                        }
+                    }
+                }
+        const double e = std::fabs(double(mass) * w / double(rho0) - 1.0);
+        sum += e;
+        mxe = std::max(mxe, e);
+        above += e > 0.1 ? 1 : 0;
+    }
+    *meanErr = n ? sum / double(n) : 0.0;
+    *maxErr = mxe;
+    if (fracAbove10) *fracAbove10 = n ? double(above) / double(n) : 0.0;
+    return ORC_OK;
 }
 
 }  // extern "C"

@@ -135,6 +135,14 @@ int orc_solver_copy_working(const orc_solver* s, orc_float4* pos, uint32_t* ids,
 /* Mean and max |rho/rho0 - 1| over the current working order and lists. */
 int orc_solver_density_error(const orc_solver* s, double* meanErr, double* maxErr);
 
+/* Density error of a set of positions, evaluated the same way whichever
+ * solver produced them: rho_i = m * sum_j W(x_i - x_j) over every particle
+ * within h (self included), poly6 in double over cells of size h; writes
+ * mean and max |rho/rho0 - 1| and the fraction of particles above 10 %. */
+int orc_density_stats(const orc_float4* pos, size_t n, orc_float3 minB, orc_float3 maxB,
+                      float h, float mass, float rho0, double* meanErr, double* maxErr,
+                      double* fracAbove10);
+
 /* ---- FP64 forward-mode restatement of the differentiated step
  * (pbf_diff_oracle.cpp): `steps` steps of integration, the density
  * constraint with s_corr and the container clamp, velocity update, XSPH and

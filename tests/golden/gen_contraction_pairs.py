@@ -7,7 +7,7 @@ particle's only candidate is its partner.  For each pair the decision is
 computed with exact rational arithmetic for nine rounding orders (fused
 multiply-add chains and the unfused sum); only pairs on which the orders
 disagree are kept.  `decisions[:, k]` is the decision under `forms[k]`.
-The reference's compiled findNeighbors (src/pbf/neighbors.cu:338-344) agrees
+The reference's compiled findNeighbors (src/pbf/neighbors.cu:73-74) agrees
 with 'z(y(xx))' = fma(dz, dz, fma(dy, dy, dx*dx)) on every pair.
 """
 

@@ -47,6 +47,29 @@ def test_batch_equals_each_scene_alone(pbf, scenes, steps, lanes):
     assert np.isfinite(mean) and mean < 0.5
 
 
+def test_batched_configuration_every_scene_equals_its_solo_run(pbf, scenes):
+    """The whole batched configuration: 256 scenes, counts log-uniform in
+    [2,048, 65,536] (4.72 M particles), block sizes chosen by the autotuner
+    as in the benchmark, 3 steps: every one of the 256 scenes bit for bit as
+    the same scene stepped by its own single-scene solver."""
+    sc, prm, pos, vel, per = scenes.batched_scenes()
+    assert len(sc) == 256
+    b = pbf.PBFSolver()
+    b.initialize_batch(sc, prm)
+    b.set_particles(pos, vel)
+    b.autotune(1)  # times trial frames, then restores the initial state
+    b.run(3)
+    bp, bv = b.copy_positions_to_host(), b.copy_velocities_to_host()
+    b.close()
+    off = 0
+    for k, (ap, av) in enumerate(run_alone(pbf, per, 3)):
+        n = len(ap)
+        np.testing.assert_array_equal(bp[off:off + n], ap, err_msg="scene %d positions" % k)
+        np.testing.assert_array_equal(bv[off:off + n], av, err_msg="scene %d velocities" % k)
+        off += n
+    assert off == len(bp)
+
+
 def test_batch_takes_exactly_all_particles(pbf, scenes):
     sc, prm, pos, vel, _ = scenes.batched_scenes(n_scenes=3, n_min=512, n_max=1024, seed=2)
     b = pbf.PBFSolver()

@@ -5,7 +5,8 @@
   stable ids, working order) -- the oracle performs the kernels' operation
   sequence with the same fused multiply-adds.
 * Within FP32 tolerance of the FP64 oracle (reference formulas in double)
-  after 1 and 10 steps, the accuracy check of the FP32 solver.
+  after 1 and 10 steps, the accuracy check of the FP32 solver
+  (check_tolerance states the bounds).
 """
 
 import numpy as np
@@ -44,6 +45,41 @@ def assert_bitwise(a, b, what):
             what, len(bad), bad[0], a[tuple(bad[0])], b[tuple(bad[0])]))
 
 
+def wall_distance(p, mn, mx, r):
+    """Distance of each particle to the nearest container wall it can touch
+    (x, z both sides, the floor; the top is open), in double."""
+    x, y, z = (p[:, k].astype(np.float64) for k in range(3))
+    return np.min(np.stack([x - (mn[0] + r), (mx[0] - r) - x, y - (mn[1] + r),
+                            z - (mn[2] + r), (mx[2] - r) - z], 1), 1)
+
+
+def check_tolerance(got_p, got_v, want_p, want_v, steps, mn, mx, r, h, what):
+    """FP32 steps against a reference state (positions in length units,
+    velocities in units/s).  After 1 step: every |dx| <= 2e-6, every
+    |dv| <= 5e-4.  After 10 steps: every |dx| <= 1e-3, the 99.9th percentile
+    <= 1e-4, at most one particle in 10,000 (at least 4) beyond 1e-4 and each
+    of those within h of a container wall -- the velocity response's 1e-4
+    contact band switches on in one precision and not in the other there, and
+    the constraint spreads the difference to the neighbours -- every |dv| <=
+    0.06 and the 99.9th percentile <= 3e-3."""
+    dp = np.abs(got_p[:, :3].astype(np.float64) - want_p[:, :3]).max(1)
+    dv = np.abs(got_v[:, :3].astype(np.float64) - want_v[:, :3]).max(1)
+    assert np.isfinite(dp).all() and np.isfinite(dv).all()
+    n = len(dp)
+    if steps == 1:
+        assert dp.max() <= 2e-6, (what, dp.max())
+        assert dv.max() <= 5e-4, (what, dv.max())
+        return
+    assert dp.max() <= 1e-3, (what, dp.max())
+    assert np.percentile(dp, 99.9) <= 1e-4, (what, np.percentile(dp, 99.9))
+    far = dp > 1e-4
+    assert far.sum() <= max(4, n // 10000), (what, int(far.sum()))
+    wd = wall_distance(got_p[far], mn, mx, r)
+    assert (wd <= h).all(), (what, wd.max())
+    assert dv.max() <= 0.06, (what, dv.max())
+    assert np.percentile(dv, 99.9) <= 3e-3, (what, np.percentile(dv, 99.9))
+
+
 @pytest.mark.parametrize("steps", [1, 10])
 def test_dam_break_16k_bit_exact_vs_fp32_oracle(pbf, scenes, orc, steps):
     s, o = make_pair(pbf, orc, scenes.dam_break_16k())
@@ -68,10 +104,10 @@ def test_reference_scene_with_colliders_bit_exact(pbf, scenes, orc):
     assert_bitwise(s.copy_velocities_to_host(), o.velocities(), "velocities")
 
 
-@pytest.mark.parametrize("steps,tol", [(1, 2e-5), (10, 1e-3)])
-def test_dam_break_16k_vs_fp64_oracle(pbf, scenes, orc, steps, tol):
-    """Positions within `tol` (absolute, length units, h = 0.1) of the FP64
-    oracle; velocities within tol / dt."""
+@pytest.mark.parametrize("steps", [1, 10])
+def test_dam_break_16k_vs_fp64_oracle(pbf, scenes, orc, steps):
+    """Positions and velocities against the FP64 oracle within the bounds of
+    check_tolerance."""
     pos, vel, mn, mx, prm, col = scenes.dam_break_16k()
     s = pbf.PBFSolver()
     s.initialize(len(pos), mn, mx, prm)
@@ -81,14 +117,9 @@ def test_dam_break_16k_vs_fp64_oracle(pbf, scenes, orc, steps, tol):
     o.initialize(len(pos), mn, mx, prm.as_dict())
     o.set_particles(pos, vel)
     assert o.run(steps) == 0
-    dp = np.abs(s.copy_positions_to_host()[:, :3] - o.positions()[:, :3])
-    dv = np.abs(s.copy_velocities_to_host()[:, :3] - o.velocities()[:, :3])
-    assert np.isfinite(dp).all()
-    # Contact switches (|x - wall| < 1e-4) may flip for a handful of particles
-    # between FP32 and FP64; bound the bulk by tol and the tail loosely.
-    assert np.percentile(dp, 99.9) <= tol, np.percentile(dp, 99.9)
-    assert np.percentile(dv, 99.9) <= tol * 60.0, np.percentile(dv, 99.9)
-    assert dp.max() <= 50 * tol
+    check_tolerance(s.copy_positions_to_host(), s.copy_velocities_to_host(), o.positions(),
+                    o.velocities(), steps, mn, mx, prm.particleRadius, prm.smoothingRadius,
+                    "vs FP64 oracle")
 
 
 def test_grid_build_bit_exact_at_1m(pbf, scenes):
