@@ -193,6 +193,7 @@ def _declare(L):
         "pbf_autotune": ([_vp, C.c_int], S),
         "pbf_block_sizes": ([_vp, C.POINTER(C.c_int), C.c_int], S),
         "pbf_walk_lanes": ([_vp, C.POINTER(C.c_int)], S),
+        "pbf_sort_tile": ([_vp, C.POINTER(C.c_int)], S),
         "pbf_set_walk_lanes": ([_vp, C.c_int], S),
         "pbf_adjoint_create": ([C.POINTER(_vp), C.c_int], S),
         "pbf_adjoint_destroy": ([_vp], None),
@@ -382,14 +383,18 @@ class PBFSolver:
                      "confine")
 
     def autotune(self, frames_per_trial: int = 2) -> dict:
-        """pbf_autotune: choose the neighbour kernels' block sizes; returns them."""
+        """pbf_autotune: choose the neighbour kernels' block sizes and the sort
+        tile; returns them."""
         self._check(self._L.pbf_autotune(self._h, int(frames_per_trial)))
         return self.block_sizes()
 
     def block_sizes(self) -> dict:
+        """Threads per block of the six tuned kernels and the sort's keys per tile."""
         out = (C.c_int * 6)()
         self._check(self._L.pbf_block_sizes(self._h, out, 6))
-        return dict(zip(self.TUNED_KERNELS, list(out)))
+        tile = C.c_int()
+        self._check(self._L.pbf_sort_tile(self._h, C.byref(tile)))
+        return dict(zip(self.TUNED_KERNELS, list(out)), sort_tile=tile.value)
 
     def walk_lanes(self) -> int:
         """Lanes per particle of the list-writing walks (pbf_walk_lanes)."""

@@ -68,7 +68,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB_PATH + ".tmp%d" % os.getpid()
-    cmd = [cc] + ARCH + ["-shared", "--cudart=static", "-o", tmp] + objs
+    cmd = [cc] + ARCH + ["-shared", "--cudart=static", "-o", tmp] + objs + ["-ldl"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

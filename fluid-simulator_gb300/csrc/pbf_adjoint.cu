@@ -1166,12 +1166,14 @@ pbf_status pbf_adjoint_set_planes(pbf_adjoint* a, const pbf_plane* planes, size_
 
 pbf_status pbf_adjoint_forward(pbf_adjoint* a, const pbf_float4* x0, const pbf_float4* v0,
                                int steps, pbf_float4* x_out, pbf_float4* v_out) {
+    const NvtxRange range("pbf_adjoint_forward");
     PBF_ADJ_GUARD(a, a->forward(x0, v0, steps, x_out, v_out));
 }
 
 pbf_status pbf_adjoint_backward(pbf_adjoint* a, const pbf_float4* grad_x, const pbf_float4* grad_v,
                                 pbf_float4* grad_x0, pbf_float4* grad_v0,
                                 double* grad_rest_density, double* grad_xsph) {
+    const NvtxRange range("pbf_adjoint_backward");
     PBF_ADJ_GUARD(a, a->backward(grad_x, grad_v, grad_x0, grad_v0, grad_rest_density, grad_xsph));
 }
 

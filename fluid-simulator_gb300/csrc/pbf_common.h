@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <array>
 #include <cstddef>
@@ -38,6 +39,17 @@ std::vector<float4> collider_records(int kind, const void* data, size_t count);
 inline void cuda_check(cudaError_t e) {
     if (e != cudaSuccess) fail(PBF_ERR_RUNTIME, cudaGetErrorString(e));
 }
+
+// An NVTX range around one entry point, for a timeline tool (Nsight Systems)
+// to show the library's calls, as the reference's benchmark marks its run and
+// every physics frame (benchmark/pbf_benchmark.cu:44,125-137).  Costs a
+// function-pointer check when no tool is attached.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // Move-only owner of one device allocation (the role CudaBuffer plays in the
 // reference, include/pbf/cuda_buffer.hpp:11-139).

@@ -171,8 +171,11 @@ struct SortPlan {
 // Smallest tile (keys) any plan uses, and the most digit bins of a pass:
 // the scratch of n keys holds (ceil(n / kSortMinTile) + 1) * kSortMaxBins words.
 constexpr int kSortMinTile = 1024;
+constexpr int kSortMaxTile = 4096;
 constexpr int kSortMaxBins = 256;
-SortPlan make_sort_plan(int n, uint64_t num_cells);
+// tile: keys per tile, kSortMinTile or kSortMaxTile; anything else picks by
+// size (the smaller tiles below 2^19 keys).  The result does not depend on it.
+SortPlan make_sort_plan(int n, uint64_t num_cells, int tile = 0);
 // Scratch bytes for hist/totals of a plan with up to n keys.
 size_t sort_scratch_bytes(int max_n);
 // Sorts keys (current order) into sorted_keys/sorted_idx; values start as the

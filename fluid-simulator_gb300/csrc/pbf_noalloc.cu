@@ -35,7 +35,10 @@ static __device__ __align__(256) unsigned char g_static_scratch[kScratchBytes];
 
 // Host code cannot use g_static_scratch directly (on the host the name is a
 // stand-in, not a device address), so its device address is looked up once
-// per device, with that device current, and cached.
+// per device, with that device current, and cached.  A cudaDeviceReset
+// unloads the library's device code with the array, after which the cached
+// address is stale: the entry point is not for use after a reset of its
+// device in the same process.
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mu;
 unsigned char* g_scratch_ptr[kMaxDevices] = {};
@@ -68,6 +71,9 @@ pbf_status pbf_grid_build_static_scratch(const pbf_float4* d_positions, size_t c
                                          uint32_t* d_sorted_indices, int* d_cell_start,
                                          int* d_cell_end, void* stream) {
     return guarded(nullptr, [&]() {
+        if (count > kStaticScratchParticles)
+            fail(PBF_ERR_LENGTH,
+                 "particle count exceeds the static scratch capacity of 262144 particles");
         if (!std::isfinite(cell_size) || cell_size <= 0.0f)
             fail(PBF_ERR_INVALID_ARGUMENT, "cellSize must be greater than zero");
         const float lo[3] = {min_bounds.x, min_bounds.y, min_bounds.z};
@@ -85,9 +91,6 @@ pbf_status pbf_grid_build_static_scratch(const pbf_float4* d_positions, size_t c
         if (size_t(d[0]) > maxCells / size_t(d[1]) ||
             size_t(d[0]) * size_t(d[1]) > maxCells / size_t(d[2]))
             fail(PBF_ERR_LENGTH, "Spatial grid exceeds 32-bit key capacity");
-        if (count > kStaticScratchParticles)
-            fail(PBF_ERR_LENGTH,
-                 "particle count exceeds the static scratch capacity of 262144 particles");
         const size_t cells = size_t(d[0]) * size_t(d[1]) * size_t(d[2]);
         if (!d_cell_start || !d_cell_end)
             fail(PBF_ERR_INVALID_ARGUMENT, "cell_start and cell_end must not be null");
@@ -115,9 +118,11 @@ pbf_status pbf_grid_build_static_scratch(const pbf_float4* d_positions, size_t c
         g.gy = d[1];
         g.gz = d[2];
         launch_grid_keys(reinterpret_cast<const float4*>(d_positions), keys, n, g, st);
-        // The sort zeroes its digit totals itself before every pass; the
-        // histograms and key buffers are fully rewritten, so nothing left in
-        // the shared array by an earlier call is read.
+        // Nothing an earlier call left in the shared array is read: every
+        // pass rewrites the tile histograms it reads (upsweep), the digit
+        // totals are either rewritten by the scan launch or, with few tiles,
+        // not read at all (the downsweep sums the histograms itself), and the
+        // key buffers are written before they are read.
         const SortPlan plan = make_sort_plan(n, cells);
         launch_sort(plan, keys, d_sorted_keys, d_sorted_indices, alt_keys, alt_idx, sort_scratch,
                     nullptr, st);

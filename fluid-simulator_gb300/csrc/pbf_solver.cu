@@ -200,6 +200,7 @@ struct pbf_solver {
     // Threads per block of the tuned kernels (0 = the default 256).
     int tuned[kTunedCount] = {};
     int tuned_lanes = 0;  // lanes per particle of the walks set by pbf_set_walk_lanes; 0 = default
+    int sort_tile = 0;    // keys per radix-sort tile chosen by the autotuner; 0 = by size
 
     // Compact neighbour lists (list_cap > 0): every rebuild counts the
     // neighbours, scans the counts into nb_off and writes each particle's
@@ -345,7 +346,7 @@ struct pbf_solver {
         };
         auto give = [&](int i) { used[i] = false; };
         auto P = [&](int i) { return f4[i].as<float4>(); };
-        const SortPlan plan = make_sort_plan(N, cells);
+        const SortPlan plan = make_sort_plan(N, cells, sort_tile);
         const bool post = prm.xsphViscosity != 0.0f || prm.vorticityStrength != 0.0f;
 
         auto M = [&](int stage) {
@@ -535,12 +536,14 @@ struct pbf_solver {
         }
     }
 
-    // Block-size autotuner: for each tuned kernel, time its stage in profiled
-    // frames at 64, 128, 256 and 512 threads per block and keep the fastest
-    // (coordinate descent, one kernel at a time; the other kernels keep their
-    // current sizes).  Block size changes no arithmetic, so results stay bit
-    // for bit the same.  The particle state is saved before and restored
-    // after, so tuning does not advance the simulation.
+    // Autotuner: for each tuned kernel, time its stage in profiled frames at
+    // 64, 128, 256 and 512 threads per block and keep the fastest (coordinate
+    // descent, one kernel at a time; the other kernels keep their current
+    // sizes); then the radix sort's tile (1,024 keys in 256-thread blocks or
+    // 4,096 keys in 512-thread blocks), timed on the sort stage.  Neither
+    // changes any arithmetic or the sort's result, so results stay bit for
+    // bit the same.  The particle state is saved before and restored after,
+    // so tuning does not advance the simulation.
     void autotune(int frames_per_trial) {
         require_initialized("PBFSolver must be initialized before tuning");
         if (n == 0) fail(PBF_ERR_LOGIC, "no particles to tune on");
@@ -553,10 +556,12 @@ struct pbf_solver {
         std::vector<int> launches(kStageCount);
         int saved[kTunedCount];
         std::copy(tuned, tuned + kTunedCount, saved);
+        const int saved_tile = sort_tile;
         try {
             tune_all(frames_per_trial, ms, launches, sx.as<float4>(), sv.as<float4>());
         } catch (...) {
             std::copy(saved, saved + kTunedCount, tuned);
+            sort_tile = saved_tile;
             clear_graphs();
             set_particles(sx.as<float4>(), sv.as<float4>(), n, true);
             throw;
@@ -605,6 +610,25 @@ struct pbf_solver {
             }
             tuned[k] = best;
         }
+        // The sort tile, timed on the sort stage of the same frames.
+        int best_tile = sort_tile;
+        float best_ms = -1.0f;
+        for (int tile : {kSortMinTile, kSortMaxTile}) {
+            sort_tile = tile;
+            clear_graphs();
+            warm_trial(ms, launches, x0, v0);
+            float t = -1.0f;
+            for (int f = 0; f < frames_per_trial; ++f) {
+                set_particles(x0, v0, n, true);
+                profile_frame(ms.data(), launches.data());
+                t = t < 0.0f ? ms[kStSort] : std::min(t, ms[kStSort]);
+            }
+            if (t >= 0.0f && (best_ms < 0.0f || t < best_ms)) {
+                best_ms = t;
+                best_tile = tile;
+            }
+        }
+        sort_tile = best_tile;
     }
 
     // Lanes per particle of the list-writing walks: the value set, else the
@@ -1018,6 +1042,7 @@ pbf_status pbf_set_planes(pbf_solver* s, const pbf_plane* p, size_t count) {
 }
 
 pbf_status pbf_step(pbf_solver* s) {
+    const NvtxRange range("pbf_step");
     PBF_GUARD(s, {
         s->require_initialized("PBFSolver must be initialized before stepping");
         s->run_frames(1, true);
@@ -1025,6 +1050,7 @@ pbf_status pbf_step(pbf_solver* s) {
 }
 
 pbf_status pbf_run(pbf_solver* s, size_t frames) {
+    const NvtxRange range("pbf_run");
     PBF_GUARD(s, {
         s->require_initialized("PBFSolver must be initialized before running");
         s->run_frames(frames, true);
@@ -1032,6 +1058,7 @@ pbf_status pbf_run(pbf_solver* s, size_t frames) {
 }
 
 pbf_status pbf_run_async(pbf_solver* s, size_t frames) {
+    const NvtxRange range("pbf_run_async");
     PBF_GUARD(s, {
         s->require_initialized("PBFSolver must be initialized before running");
         s->run_frames(frames, false);
@@ -1047,6 +1074,7 @@ pbf_status pbf_synchronize(pbf_solver* s) {
 }
 
 pbf_status pbf_time_frames(pbf_solver* s, size_t frames, float* ms) {
+    const NvtxRange range("pbf_time_frames");
     PBF_GUARD(s, {
         s->require_initialized("PBFSolver must be initialized before running");
         if (!ms) fail(PBF_ERR_INVALID_ARGUMENT, "milliseconds must not be null");
@@ -1131,6 +1159,16 @@ pbf_status pbf_block_sizes(const pbf_solver* s, int* sizes, int count) {
     }
     for (int k = 0; k < count && k < kTunedCount; ++k)
         sizes[k] = s->tuned[k] > 0 ? s->tuned[k] : kBlock;
+    return PBF_OK;
+}
+
+pbf_status pbf_sort_tile(const pbf_solver* s, int* keys_per_tile) {
+    if (!s || !keys_per_tile) {
+        pbf::set_global_error("solver handle and keys_per_tile must not be null");
+        return PBF_ERR_INVALID_ARGUMENT;
+    }
+    *keys_per_tile = make_sort_plan(static_cast<int>(std::min<size_t>(s->n, 1u << 30)),
+                                    uint64_t(1), s->sort_tile).tile;
     return PBF_OK;
 }
 

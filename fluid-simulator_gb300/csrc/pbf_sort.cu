@@ -246,10 +246,13 @@ k_downsweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ v
 
 }  // namespace
 
-SortPlan make_sort_plan(int n, uint64_t num_cells) {
+SortPlan make_sort_plan(int n, uint64_t num_cells, int tile) {
     SortPlan p;
     p.n = n;
-    p.tile = n < kSmallTileBelow ? Small::kTile : Large::kTile;
+    if (tile == Small::kTile || tile == Large::kTile)
+        p.tile = tile;
+    else
+        p.tile = n < kSmallTileBelow ? Small::kTile : Large::kTile;
     p.tiles = std::max(1, (n + p.tile - 1) / p.tile);
     int bits = 1;
     while (bits < 32 && (uint64_t(1) << bits) < num_cells) ++bits;

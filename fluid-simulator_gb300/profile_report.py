@@ -1,8 +1,13 @@
 """Per-kernel profile of one PBF frame with Nsight Compute.
 
 The counterpart of the reference's ``benchmark/profile.py`` (nsys + ncu), with
-no disassembly step.  Two kinds of ncu runs, both with ``--clock-control
-none``:
+no disassembly step.  A timeline section first: with Nsight Systems on the
+PATH, ``nsys profile --trace=cuda,nvtx`` of the same workload and its NVTX
+range and kernel summaries (the library marks pbf_step, pbf_run,
+pbf_run_async, pbf_time_frames and the adjoint's forward and backward with
+NVTX ranges); without it, the frame's stages timed by CUDA events recorded
+inside the frame graph (pbf_profile_frame), in pipeline order.  Then two
+kinds of ncu runs, both with ``--clock-control none``:
 
 1. a launch list of one whole frame (``gpu__time_duration.sum`` only, a
    single replay pass): launches, device time and share per kernel;
@@ -72,6 +77,73 @@ def child(scene: str, warmup: int, frames: int):
     print("kernels_per_frame %d" % s.kernels_per_frame(), flush=True)
 
 
+def child_stages(scene: str, warmup: int):
+    """Stage times of one frame from CUDA events inside the frame graph,
+    printed one stage per line in pipeline order: name, ms, launches."""
+    pkg = load_pkg()
+    scenes = importlib.import_module("fluid_simulator_gb300.scenes")
+    pos, vel, mn, mx, prm, col = scenes.SCENES[scene]()
+    s = pkg.PBFSolver()
+    s.initialize(len(pos), mn, mx, prm)
+    for k, fn in (("spheres", s.set_spheres), ("boxes", s.set_boxes), ("planes", s.set_planes)):
+        if col.get(k):
+            fn(col[k])
+    s.set_particles(pos, vel)
+    s.run(warmup)
+    s.profile_frame()  # records the profiled graph
+    for name, (ms, launches) in s.profile_frame().items():
+        print("stage %s %.6f %d" % (name, ms, launches), flush=True)
+
+
+def timeline(args, me, shown, tmp):
+    """Report lines of the timeline section (see the module docstring)."""
+    import shutil
+    nsys = shutil.which(args.nsys)
+    if nsys:
+        rep = os.path.join(tmp, "timeline")
+        cmd = [nsys, "profile", "--trace=cuda,nvtx", "--sample=none", "--cpuctxsw=none",
+               "--force-overwrite=true", "-o", rep] + me
+        run(cmd)
+        lines = ["## Timeline (Nsight Systems)", "", "    " + shown(cmd), ""]
+        for report in ("nvtx_sum", "cuda_gpu_kern_sum"):
+            base = os.path.join(tmp, "stats")
+            run([nsys, "stats", "--report", report, "--format", "csv", "--force-export=true",
+                 "--output", base, rep + ".nsys-rep"])
+            path = [os.path.join(tmp, f) for f in os.listdir(tmp)
+                    if f.startswith("stats") and report in f and f.endswith(".csv")]
+            if not path:
+                continue
+            rows = list(csv.reader(open(path[0])))
+            if not rows:
+                continue
+            lines += ["### " + report, "", "| " + " | ".join(rows[0]) + " |",
+                      "|" + "---|" * len(rows[0])]
+            lines += ["| " + " | ".join(r) + " |" for r in rows[1:40]]
+            lines.append("")
+        return lines
+    if args.adjoint:
+        return ["## Timeline", "", "Nsight Systems (%s) is not installed here; the adjoint "
+                "has no stage timeline." % args.nsys, ""]
+    cmd = [sys.executable, os.path.abspath(__file__), "--child", "--stages", "--scene",
+           args.scene, "--warmup", str(args.warmup)]
+    out = run(cmd)
+    lines = ["## Timeline (CUDA events inside the frame graph)", "",
+             "Nsight Systems (%s) is not installed here.  One frame's stages, timed by CUDA "
+             "events recorded between them in the profiled frame graph, in pipeline order "
+             "(warm caches, graph launch):" % args.nsys, "", "    " + shown(cmd), "",
+             "| stage | launches | ms | starts at ms (stages in order) | share |",
+             "|---|---|---|---|---|"]
+    stages = [l.split()[1:] for l in out.splitlines() if l.startswith("stage ")]
+    total = sum(float(t) for _, t, _ in stages) or 1.0
+    at = 0.0
+    for name, t, n in stages:
+        lines.append("| %s | %s | %.4f | %.4f | %.1f%% |" % (name, n, float(t), at,
+                                                           100.0 * float(t) / total))
+        at += float(t)
+    lines.append("")
+    return lines
+
+
 def child_adjoint(steps: int):
     """The profiled adjoint workload: 65,536 particles (64x64x16 dam-break
     lattice, the 1M dam break's parameters: XSPH and vorticity confinement
@@ -133,6 +205,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=2)
     ap.add_argument("--top", type=int, default=4)
     ap.add_argument("--ncu", default="ncu")
+    ap.add_argument("--nsys", default="nsys")
+    ap.add_argument("--stages", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--out", default=None)
     ap.add_argument("--adjoint", action="store_true",
                     help="profile the adjoint (forward + backward of --adjoint-steps steps at "
@@ -143,6 +217,8 @@ def main():
     if args.child:
         if args.adjoint:
             child_adjoint(args.adjoint_steps)
+        elif args.stages:
+            child_stages(args.scene, args.warmup)
         else:
             child(args.scene, args.warmup, 1)
         return 0
@@ -169,6 +245,8 @@ def main():
 
     out = run(me)  # plain run first: it must succeed before ncu sees it
     kpf = int(out.split("kernels_per_frame")[1].split()[0])
+    tmp_tl = tempfile.mkdtemp(prefix="pbf_tl_")
+    tl_lines = timeline(args, me, shown, tmp_tl)
     # Solver: skip set_particles (two kernels) and the warm-up frames, list
     # one frame.  Adjoint: list every launch of the forward and backward.
     before = 0 if args.adjoint else 2 + args.warmup * kpf
@@ -222,7 +300,9 @@ def main():
     lines = [title, "", "Generated by:", "", gen, "",
              "which runs (each after the same workload exited 0 without ncu):", ""]
     lines += ["    " + c for c in cmds]
-    lines += ["", "| kernel | %s | device us | share |" % unit, "|---|---|---|---|"]
+    lines += [""] + tl_lines
+    lines += ["## Launch list (ncu)", "", "| kernel | %s | device us | share |" % unit,
+              "|---|---|---|---|"]
     for k, (cnt, sec, _) in order:
         lines.append("| %s | %d | %.1f | %.1f%% |" % (k, cnt, sec * 1e6, 100.0 * sec / total))
     lines += ["", "Top kernels, one launch each:", "",

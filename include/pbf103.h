@@ -155,16 +155,20 @@ pbf_status pbf_batch_initialize(pbf_solver* s, const pbf_scene* scenes, int scen
 /* Scenes of a batched handle (0 after pbf_initialize). */
 int pbf_batch_scene_count(const pbf_solver* s);
 
-/* Block-size autotuner (no counterpart in the reference): for the six
- * neighbour kernels (walk + lambda, delta p, final walk, XSPH, vorticity,
+/* Autotuner (no counterpart in the reference): for the six neighbour
+ * kernels (walk + lambda, delta p, final walk, XSPH, vorticity,
  * confinement), times each at 64, 128, 256 and 512 threads per block in profiled
  * frames (`frames_per_trial` per size, after two untimed frames) and keeps
- * the fastest.  Results do not change (block size changes no arithmetic);
- * the particle state is restored, so tuning does not advance the simulation.
- * Needs particles set. */
+ * the fastest; then the radix sort's tile, 1,024 or 4,096 keys, timed on the
+ * sort stage.  Results do not change (neither changes any arithmetic or the
+ * sort's result); the particle state is restored, so tuning does not advance
+ * the simulation.  Needs particles set. */
 pbf_status pbf_autotune(pbf_solver* s, int frames_per_trial);
 /* The block sizes in use, in the order above (count <= 6 entries). */
 pbf_status pbf_block_sizes(const pbf_solver* s, int* sizes, int count);
+/* Keys per radix-sort tile in use: 1,024 or 4,096 (chosen by the autotuner,
+ * else 1,024 below 2^19 particles and 4,096 from there on). */
+pbf_status pbf_sort_tile(const pbf_solver* s, int* keys_per_tile);
 /* Lanes per particle of the list-writing walks in use: the value set by
  * pbf_set_walk_lanes, else 4 below 32,768 particles and 1 from there on (always 1 with
  * compact lists; at most max_neighbors). */
@@ -327,10 +331,13 @@ pbf_status pbf_resolve_velocities(const pbf_float4* positions,
  * without waiting for it.  Its working memory is one fixed array inside the
  * library, pbf_static_scratch_capacity() particles large (262,144), which every
  * GPU that loads the library keeps until the process exits; larger counts are
- * rejected with PBF_ERR_LENGTH.  The first call on a device looks up that
- * array's device address (make it before any stream capture).  All calls share
- * the array: calls whose GPU work overlaps in time race and must be ordered
- * by the caller (for example by issuing them on one stream). */
+ * rejected with PBF_ERR_LENGTH before any other argument is checked.  The
+ * first call on a device looks up that array's device address (make it before
+ * any stream capture); the address is kept for the process, so the entry
+ * point must not be used on a device after cudaDeviceReset of that device.
+ * All calls share the array: calls whose GPU work overlaps in time race and
+ * must be ordered by the caller (for example by issuing them on one
+ * stream). */
 pbf_status pbf_grid_build_static_scratch(const pbf_float4* d_positions, size_t count,
                                          pbf_float3 min_bounds, pbf_float3 max_bounds,
                                          float cell_size, uint32_t* d_sorted_keys,

@@ -102,8 +102,9 @@ def test_batch_one_launch_per_stage(pbf, scenes):
 
 
 def test_autotune_keeps_results_and_state(pbf, scenes):
-    """pbf_autotune picks block sizes among 64/128/256/512, leaves the particle
-    state where it was and changes no result bit."""
+    """pbf_autotune picks block sizes among 64/128/256/512 and a sort tile of
+    1,024 or 4,096 keys, leaves the particle state where it was and changes
+    no result bit."""
     pos, vel, mn, mx, prm, _ = scenes.dam_break_16k()
     a = pbf.PBFSolver()
     a.initialize(len(pos), mn, mx, prm)
@@ -112,6 +113,7 @@ def test_autotune_keeps_results_and_state(pbf, scenes):
     x0, v0 = a.copy_positions_to_host(), a.copy_velocities_to_host()
     assert a.walk_lanes() == 4  # default below 32,768 particles
     sizes = a.autotune(1)
+    assert sizes.pop("sort_tile") in (1024, 4096)
     assert set(sizes.values()) <= {64, 128, 256, 512}
     assert a.walk_lanes() == 4  # the tuner leaves the lanes alone
     np.testing.assert_array_equal(a.copy_positions_to_host(), x0)
