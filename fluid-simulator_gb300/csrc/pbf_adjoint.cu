@@ -701,7 +701,7 @@ struct pbf_adjoint {
     int* CN(int t, int k) { return tcn.as<int>() + (static_cast<size_t>(t) * (iters + 1) + k) * n; }
     float4* SX(int j) { return states.as<float4>() + static_cast<size_t>(2 * j) * n; }
     float4* SV(int j) { return states.as<float4>() + static_cast<size_t>(2 * j + 1) * n; }
-    size_t soa_stride() const { return (n + 1 + 63) / 64 * 64; }
+    size_t soa_stride() const { return soa_stride_for(n); }
 
     void initialize(size_t count, pbf_float3 lo, pbf_float3 hi, const pbf_params& p, int maxnb,
                     int ckpt_every) {
@@ -762,6 +762,7 @@ struct pbf_adjoint {
         c.max_nb = max_nb;
         c.stride = stride;
         c.walk_lanes = default_walk_lanes(n, max_nb);
+        c.prune_cells = true;
         c.col.cminx = lo.x;
         c.col.cminy = lo.y;
         c.col.cminz = lo.z;

@@ -39,6 +39,16 @@ void launch_error_check(cudaError_t e) { cuda_check(e); }
 // spills, 6 % faster at 1M particles).
 #define PBF_GATHER_REGS(r) __maxnreg__(r)
 
+// Register budget of the list-writing walks (k_search, k_count,
+// k_search_xsph and their split forms): the 16-candidate test keeps twelve
+// 16-byte loads in flight, so the walk trades registers against resident
+// warps.  PBF_WALK_REGS (a build flag) caps it for measurements.
+#ifdef PBF_WALK_REGS
+#define PBF_WALK_BOUNDS __maxnreg__(PBF_WALK_REGS)
+#else
+#define PBF_WALK_BOUNDS __launch_bounds__(kMaxTunedBlock)
+#endif
+
 namespace {
 
 __device__ __forceinline__ bool fatal(const unsigned* status) {
@@ -261,6 +271,21 @@ __device__ __forceinline__ float lambda_finish(const StepConst& c, const LambdaA
     return lambda_finish(c.mass, c.rho0, c.gs2, c.lambda_eps, a);
 }
 
+// Squared distances from coordinate p to the slabs of the cells below and
+// above cell k on one axis (cell k spans [lo + k cell, lo + (k + 1) cell);
+// the clamped end cells extend to infinity, which changes neither distance),
+// each first reduced by eps.  Margin arithmetic only: it decides which cells
+// the walk reads, never a neighbour.
+__device__ __forceinline__ void slab_dist2(float p, float lo, float cell, int k, float eps,
+                                           float& below, float& above) {
+    const float b0 = fmaf(static_cast<float>(k), cell, lo);
+    const float b1 = fmaf(static_cast<float>(k + 1), cell, lo);
+    const float d0 = fmaxf(p - b0 - eps, 0.0f);
+    const float d1 = fmaxf(b1 - p - eps, 0.0f);
+    below = d0 * d0;
+    above = d1 * d1;
+}
+
 // The neighbour walk of particle i (position pi): writes the list slot-major
 // at out[slot * stride] (at most cap entries) and returns the full count.
 // STORE = false counts the hits without writing the list.  With PARTS > 1
@@ -285,42 +310,85 @@ __device__ __forceinline__ int walk(const StepConst& c, int i, float4 pi,
     // the reference's 64-bit key arithmetic truncates to the same values.
     const uint32_t gx = static_cast<uint32_t>(g.gx);
     const uint32_t gxy = gx * static_cast<uint32_t>(g.gy);
-    const float h2 = c.k.h2;
+    // The hit test d2 <= h2 as a sign bit: for finite d2 it holds exactly
+    // when d2 - h2u < 0, h2u being the float just above h2 (the difference
+    // of two distinct floats is never zero, and +inf or NaN, the canonical
+    // NaN of the FP32 units, give a clear sign bit: no hit, as d2 <= h2).
+    const f32x2 h2u = splat2(__uint_as_float(__float_as_uint(c.k.h2) + 1u));
     const size_t stride = nb_step(c);
-    const f32x2 px = pack2(pi.x, pi.x), py = pack2(pi.y, pi.y), pz = pack2(pi.z, pi.z);
+    const f32x2 px = splat2(pi.x), py = splat2(pi.y), pz = splat2(pi.z);
+    // Cell pruning (radius 1): a stencil cell whose box lies farther than h
+    // from the particle holds no neighbour, so the rows (y, z) and the end
+    // cells of a row that are that far are not read.  Per axis, eps =
+    // 2^-14 (|p| + |min| + cell) covers the FP32 rounding of every cell
+    // index (floor((p - min) / cell)) and of the candidates' differences,
+    // and the bound h2 (1 + 2^-10) the rounding of d2: only certain misses
+    // are left out, so the list is entry for entry the unpruned walk's.
+    const bool prune = c.prune_cells && R == 1;
+    float xb2 = 0.0f, xa2 = 0.0f, yb2 = 0.0f, ya2 = 0.0f, zb2 = 0.0f, za2 = 0.0f, lim2 = 0.0f;
+    if (prune) {
+        const float eps = 6.103515625e-05f *
+                          (fabsf(pi.x) + fabsf(pi.y) + fabsf(pi.z) + fabsf(g.minx) +
+                           fabsf(g.miny) + fabsf(g.minz) + g.cell);
+        slab_dist2(pi.x, g.minx, g.cell, cx, eps, xb2, xa2);
+        slab_dist2(pi.y, g.miny, g.cell, cy, eps, yb2, ya2);
+        slab_dist2(pi.z, g.minz, g.cell, cz, eps, zb2, za2);
+        lim2 = c.k.h2 * 1.0009765625f;
+    }
     int count = 0;
-    // Rows z -> y; inside a row the cells x0..x1 are consecutive keys, so the
+    // 16 candidates from j (a multiple of 4): the x, y, z arrays are read
+    // four floats at a time and tested two at a time with FP32x2
+    // arithmetic; each test's sign bit is shifted into acc (the first
+    // candidate ends up highest).
+    auto test16 = [&](int j, uint32_t& acc) {
+#pragma unroll
+        for (int q = 0; q < 16; q += 4) {
+            const float4 X = __ldg(reinterpret_cast<const float4*>(sx + j + q));
+            const float4 Y = __ldg(reinterpret_cast<const float4*>(sy + j + q));
+            const float4 Z = __ldg(reinterpret_cast<const float4*>(sz + j + q));
+            const f32x2 da = dist2x2(sub2(px, pack2(X.x, X.y)), sub2(py, pack2(Y.x, Y.y)),
+                                     sub2(pz, pack2(Z.x, Z.y)));
+            const f32x2 db = dist2x2(sub2(px, pack2(X.z, X.w)), sub2(py, pack2(Y.z, Y.w)),
+                                     sub2(pz, pack2(Z.z, Z.w)));
+            float a0, a1, b0, b1;
+            unpack2(sub2(da, h2u), a0, a1);
+            unpack2(sub2(db, h2u), b0, b1);
+            acc = __funnelshift_l(__float_as_uint(a0), acc, 1);
+            acc = __funnelshift_l(__float_as_uint(a1), acc, 1);
+            acc = __funnelshift_l(__float_as_uint(b0), acc, 1);
+            acc = __funnelshift_l(__float_as_uint(b1), acc, 1);
+        }
+    };
+    // Rows z -> y; inside a row the cells xa..xb are consecutive keys, so the
     // candidates of the row are one index range walked in ascending order --
     // exactly the reference's z -> y -> x cell walk (neighbors.cu:52-86).
-    // Each range is scanned in 32-candidate chunks starting at an even index:
-    // pairs of candidates are tested with FP32x2 arithmetic on the component
-    // arrays (8-byte loads), the results go into a hit mask without branches,
-    // and the hits are then appended in ascending order.  Candidates outside
-    // [s, e) and the particle itself are masked off; the component arrays
-    // are padded so the odd element past e is always readable.
+    // Each range is tested in 32-candidate chunks from a multiple of 4 (the
+    // second half of a chunk only if the range reaches it); candidates
+    // outside [s, e) and the particle itself are masked off, and the hits
+    // are then appended in ascending order.  The component arrays are padded
+    // (soa_stride_for), so a chunk may read past the last particle.
     auto row_walk = [&](int z, int y) {
+        int xa = x0, xb = x1;
+        if (prune) {
+            const float dyz = (z < cz ? zb2 : (z > cz ? za2 : 0.0f)) +
+                              (y < cy ? yb2 : (y > cy ? ya2 : 0.0f));
+            if (dyz > lim2) return;
+            if (xa < cx && dyz + xb2 > lim2) xa = cx;
+            if (xb > cx && dyz + xa2 > lim2) xb = cx;
+        }
         const uint32_t row =
             base + static_cast<uint32_t>(y) * gx + static_cast<uint32_t>(z) * gxy;
-        const int s = __ldg(&first[row + static_cast<uint32_t>(x0)]);
-        const int e = __ldg(&first[row + static_cast<uint32_t>(x1) + 1u]);
-        for (int j0 = s & ~1; j0 < e; j0 += 32) {
-            const int lim = min(32, e - j0);
-            uint32_t mask = 0u;
-#pragma unroll 4
-            for (int b = 0; b < lim; b += 2) {
-                const float2 X = __ldg(reinterpret_cast<const float2*>(sx + j0 + b));
-                const float2 Y = __ldg(reinterpret_cast<const float2*>(sy + j0 + b));
-                const float2 Z = __ldg(reinterpret_cast<const float2*>(sz + j0 + b));
-                const f32x2 d2 = dist2x2(sub2(px, pack2(X.x, X.y)),
-                                         sub2(py, pack2(Y.x, Y.y)),
-                                         sub2(pz, pack2(Z.x, Z.y)));
-                float da, db;
-                unpack2(d2, da, db);
-                mask |= (static_cast<uint32_t>(da <= h2) |
-                         (static_cast<uint32_t>(db <= h2) << 1)) << b;
-            }
+        const int s = __ldg(&first[row + static_cast<uint32_t>(xa)]);
+        const int e = __ldg(&first[row + static_cast<uint32_t>(xb) + 1u]);
+        for (int j0 = s & ~3; j0 < e; j0 += 32) {
+            const int left = e - j0;
+            uint32_t acc = 0u;
+            test16(j0, acc);
+            if (left > 16) test16(j0 + 16, acc);
+            else acc <<= 16;
+            uint32_t mask = __brev(acc);
             // Keep bits of [s, e) only, and drop the particle itself.
-            uint32_t valid = lim >= 32 ? 0xffffffffu : ((1u << lim) - 1u);
+            uint32_t valid = left >= 32 ? 0xffffffffu : ((1u << left) - 1u);
             if (j0 < s) valid &= ~((1u << (s - j0)) - 1u);
             const int self = i - j0;
             if (self >= 0 && self < 32) valid &= ~(1u << self);
@@ -418,7 +486,7 @@ __device__ __forceinline__ void search_tail(const StepConst& c, int i, float4 pi
 }
 
 template <bool LAMBDA, bool B>
-__global__ void __launch_bounds__(kMaxTunedBlock)
+__global__ void PBF_WALK_BOUNDS
 k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
          const float* __restrict__ sy, const float* __restrict__ sz, const int* __restrict__ first,
          StepConst c, int n, uint32_t* __restrict__ nbr, int* __restrict__ cnt,
@@ -490,7 +558,7 @@ __device__ __forceinline__ unsigned lane_group_mask() {
 // GPU with one thread per particle, where a walk is bound by the latency of
 // one thread's row after row.
 template <bool LAMBDA, bool B, int L>
-__global__ void __launch_bounds__(kMaxTunedBlock)
+__global__ void PBF_WALK_BOUNDS
 k_search_split(const float4* __restrict__ xs, const float* __restrict__ sx,
                const float* __restrict__ sy, const float* __restrict__ sz,
                const int* __restrict__ first, StepConst c, int n, uint32_t* __restrict__ nbr,
@@ -508,7 +576,7 @@ k_search_split(const float4* __restrict__ xs, const float* __restrict__ sx,
 
 // Compact lists, first pass: the walk's neighbour count only.
 template <bool B>
-__global__ void __launch_bounds__(kMaxTunedBlock)
+__global__ void PBF_WALK_BOUNDS
 k_count(const float4* __restrict__ xs, const float* __restrict__ sx,
         const float* __restrict__ sy, const float* __restrict__ sz,
         const int* __restrict__ first, StepConst c, int n, int* __restrict__ cnt,
@@ -875,7 +943,7 @@ __device__ __forceinline__ void xsph_tail(const StepConst& c, int i, float4 pi,
 // updated ones, computed before this walk), with the velocity response when
 // no vorticity pass follows.
 template <bool B>
-__global__ void __launch_bounds__(kMaxTunedBlock)
+__global__ void PBF_WALK_BOUNDS
 k_search_xsph(const float4* __restrict__ xs, const float* __restrict__ sx,
               const float* __restrict__ sy, const float* __restrict__ sz,
               const int* __restrict__ first, StepConst c, int n, uint32_t* __restrict__ nbr,
@@ -891,7 +959,7 @@ k_search_xsph(const float4* __restrict__ xs, const float* __restrict__ sx,
 // k_search_xsph with L lanes per particle for the walk; lane 0 of each group
 // applies XSPH (see k_search_split).
 template <bool B, int L>
-__global__ void __launch_bounds__(kMaxTunedBlock)
+__global__ void PBF_WALK_BOUNDS
 k_search_xsph_split(const float4* __restrict__ xs, const float* __restrict__ sx,
                     const float* __restrict__ sy, const float* __restrict__ sz,
                     const int* __restrict__ first, StepConst c, int n,

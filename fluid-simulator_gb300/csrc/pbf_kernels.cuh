@@ -47,11 +47,24 @@ struct StepConst {
     // than one splits each particle's stencil rows over a lane group, for
     // scenes too small to fill the GPU.  Slot-major lists only.
     int walk_lanes;
+    // Leave out of the walks the stencil cells that cannot hold a neighbour
+    // (their box is farther than h from the particle).  Needs cell tables
+    // built from the walked positions themselves, as the step's rebuilds
+    // are; off for the stage entry points, which take the caller's tables.
+    bool prune_cells;
 };
 
 // Lanes per particle for the walks of an n-particle scene (slot-major lists
 // with max_nb slots).
 int default_walk_lanes(size_t n, int max_nb);
+
+// Stride (floats) of the x, y, z component arrays the walks read, for n
+// particles: a multiple of 64 (every array 256-byte aligned, so the walk's
+// 16-byte loads are aligned) with at least kSoaTail readable floats past the
+// last particle, because the walk tests candidates in 32-wide chunks that
+// may run past the end of a cell row (those lanes are masked off).
+constexpr size_t kSoaTail = 32;
+constexpr size_t soa_stride_for(size_t n) { return (n + kSoaTail + 63) / 64 * 64; }
 
 // Kernels whose block size the solver's autotuner chooses.
 enum TunedKernel { kTunedSearchLambda, kTunedDelta, kTunedSearch, kTunedXsph, kTunedVorticity,

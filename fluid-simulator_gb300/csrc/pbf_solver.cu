@@ -215,10 +215,8 @@ struct pbf_solver {
     DeviceBuffer keys, skeys, sidx, akeys, aidx;
     DeviceBuffer cell_first, nbr, cnt, lam, sort_scratch, status, tmp4, ftmp;
     DeviceBuffer soa;  // x, y, z components of the reordered predicted positions
-    // Component array stride: a multiple of 64 floats, so every array starts
-    // 256-byte aligned and the search's even-index pair loads are 8-byte
-    // aligned; at least cap + 1 so a pair may read one element past the end.
-    size_t soa_stride() const { return (cap + 1 + 63) / 64 * 64; }
+    // Component array stride (see soa_stride_for).
+    size_t soa_stride() const { return soa_stride_for(cap); }
     unsigned* h_status = nullptr;
     int ix = 0, iv = 1, iid = 0;  // roles: positions, velocities, ids
 
@@ -307,6 +305,7 @@ struct pbf_solver {
             c.nb_cap = list_cap;
         }
         c.walk_lanes = walk_lanes();
+        c.prune_cells = true;
         return c;
     }
 
@@ -709,7 +708,7 @@ struct pbf_solver {
         for (auto& b : norg) b.allocate(u4b);
         DeviceBuffer nkeys(u4b), nskeys(u4b), nsidx(u4b), nakeys(u4b), naidx(u4b);
         DeviceBuffer nfirst((ncells + 1) * sizeof(int));
-        DeviceBuffer nsoa(3 * ((max_particles + 1 + 63) / 64 * 64) * sizeof(float));
+        DeviceBuffer nsoa(3 * soa_stride_for(max_particles) * sizeof(float));
         DeviceBuffer nnbr((lcap > 0 ? lcap : strd * size_t(maxnb)) * sizeof(uint32_t));
         DeviceBuffer nnboff, nnbscr;
         if (lcap > 0) {

@@ -212,10 +212,9 @@ pbf_status pbf_find_neighbors(const pbf_float4* sorted_positions, size_t count,
         StepConst c = kernel_const(h, 1.0f, 1.0f, max_neighbors, stride);
         c.k.h2 = h * h;
         c.g = grid_const(mn, cell, dims, h);
-        // Component arrays for the search (identity gather of the given order).
-        // Padded to 64 floats per component so pair loads stay 8-byte aligned,
-        // with room for the element a pair may read past the end.
-        const size_t pad = (count + 1 + 63) / 64 * 64;
+        // Component arrays for the search (identity gather of the given order),
+        // padded as the walk needs (soa_stride_for).
+        const size_t pad = soa_stride_for(count);
         DeviceBuffer dsoa(3 * pad * sizeof(float)), dids(count * sizeof(uint32_t)),
             dcopy(count * sizeof(float4));
         launch_iota(dids.as<uint32_t>(), static_cast<int>(count), nullptr);
