@@ -75,15 +75,21 @@ STAGE_BYTES = {
 
 
 # ncu captures of the dominant kernel (k_search<1>: walk + lambda) on the
-# 1M dam break, one launch each, keyed by the frame they were taken at:
+# 1M dam break, keyed by frame: the mean over the frame's four launches of
 # DRAM bytes read + written (dram__bytes_read.sum + dram__bytes_write.sum)
-# and warp instructions (smsp__inst_executed.sum).  A timed window is matched
-# with the capture nearest its middle frame; the line names that frame.
+# and warp instructions (smsp__inst_executed.sum), from
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,smsp__inst_executed.sum,
+#       gpu__time_duration.sum --clock-control none --kernel-name-base demangled
+#       -k 'regex:k_search<.bool.1' -s <4 (F - 1)> -c 4
+#       python fluid-simulator_gb300/profile_report.py --child --scene dam_break_1m
+#       --warmup <F - 1>
+# A timed window is matched with the capture nearest its middle frame; the
+# line names that frame.
 CAPTURES = {
     "search_lambda": {
-        16: {"dram_bytes": 64.153344e6 + 99.089664e6, "inst": 191478667.0},
-        106: {"dram_bytes": 125.748480e6 + 214.701568e6, "inst": 293904341.0},
-        150: {"dram_bytes": 103.668736e6 + 165.316864e6, "inst": 245930457.0},
+        16: {"dram_bytes": 60.676864e6 + 94.141632e6, "inst": 163705114.0},
+        106: {"dram_bytes": 111.414400e6 + 199.216960e6, "inst": 245673552.0},
+        150: {"dram_bytes": 95.744576e6 + 158.054208e6, "inst": 207600024.0},
     },
 }
 SMS, ISSUE_PER_SM_CLK = 152, 4
@@ -112,7 +118,7 @@ def issue_roofline(kernel, ms_per_launch, clocks, scene, mid_frame):
             "unit": "G warp-instructions/s", "frac": achieved / peak,
             "inst_per_launch": cap["inst"], "captured_at_frame": frame,
             "window_mid_frame": mid_frame,
-            "source": "smsp__inst_executed.sum of one ncu capture (--clock-control none)"}
+            "source": "smsp__inst_executed.sum, mean of the frame's four launches in one ncu capture (--clock-control none)"}
 
 
 def load_pkg():
