@@ -288,15 +288,12 @@ __device__ __forceinline__ void slab_dist2(float p, float lo, float cell, int k,
 
 // The neighbour walk of particle i (position pi): writes the list slot-major
 // at out[slot * stride] (at most cap entries) and returns the full count.
-// STORE = false counts the hits without writing the list.  With PARTS > 1
-// only rows [part * rows / PARTS, (part + 1) * rows / PARTS) of the stencil
-// are walked (rows in z -> y order), so the lists of parts 0, 1, ...
-// concatenated are the whole list.  (PARTS = parts.)
-template <bool B, bool STORE = true, int PARTS = 1>
+// STORE = false counts the hits without writing the list.
+template <bool B, bool STORE = true>
 __device__ __forceinline__ int walk(const StepConst& c, int i, float4 pi,
                                     const float* __restrict__ sx, const float* __restrict__ sy,
                                     const float* __restrict__ sz, const int* __restrict__ first,
-                                    uint32_t* __restrict__ out, int cap, int part = 0) {
+                                    uint32_t* __restrict__ out, int cap) {
     GridConst g;
     uint32_t base;
     grid_of<B>(c, i, g, base);
@@ -407,23 +404,8 @@ __device__ __forceinline__ int walk(const StepConst& c, int i, float4 pi,
             }
         }
     };
-    if constexpr (PARTS == 1) {
-        for (int z = z0; z <= z1; ++z)
-            for (int y = y0; y <= y1; ++y) row_walk(z, y);
-    } else {
-        const int ny = y1 - y0 + 1;
-        const int rows = ny * (z1 - z0 + 1);
-        const int r_end = (part + 1) * rows / PARTS;
-        int r = part * rows / PARTS;
-        int z = z0 + r / ny, y = y0 + r % ny;
-        for (; r < r_end; ++r) {
-            row_walk(z, y);
-            if (++y > y1) {
-                y = y0;
-                ++z;
-            }
-        }
-    }
+    for (int z = z0; z <= z1; ++z)
+        for (int y = y0; y <= y1; ++y) row_walk(z, y);
     return count;
 }
 
@@ -499,53 +481,134 @@ k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
     search_tail<LAMBDA, B>(c, i, pi, xs, out, count, cnt, lam, status);
 }
 
-// Split walk: the L lanes of a group (consecutive lanes, gmask) walk
-// consecutive parts of particle i's stencil rows.  Part `sub` writes its hits
-// into slots [sub * P, (sub + 1) * P) of the particle's slot-major list
-// (P = max_nb / L); the parts are then moved down to their final slots in
-// part order, so the list is the one walk<B> writes, entry for entry.  If a
-// part holds more than P hits (and the whole list fits), lane 0 walks all
-// rows again.  Returns the full count on every lane of the group.
+// The stencil rows of particle i, as the walk visits them: range(z, y)
+// gives row (z, y)'s candidate index range [s, e), false where cell
+// pruning leaves the row out (the same decisions as walk()).
+template <bool B>
+struct StencilRows {
+    GridConst g;
+    uint32_t base, gx, gxy;
+    int cx, cy, cz, x0, x1, y0, y1, z0, z1;
+    bool prune;
+    float xb2, xa2, yb2, ya2, zb2, za2, lim2;
+    __device__ __forceinline__ StencilRows(const StepConst& c, int i, float4 pi) {
+        grid_of<B>(c, i, g, base);
+        cell_of(g, pi.x, pi.y, pi.z, cx, cy, cz);
+        const int R = g.radius;
+        x0 = max(0, cx - R);
+        x1 = min(g.gx - 1, cx + R);
+        y0 = max(0, cy - R);
+        y1 = min(g.gy - 1, cy + R);
+        z0 = max(0, cz - R);
+        z1 = min(g.gz - 1, cz + R);
+        gx = static_cast<uint32_t>(g.gx);
+        gxy = gx * static_cast<uint32_t>(g.gy);
+        prune = c.prune_cells && R == 1;
+        xb2 = xa2 = yb2 = ya2 = zb2 = za2 = lim2 = 0.0f;
+        if (prune) {
+            const float eps = 6.103515625e-05f *
+                              (fabsf(pi.x) + fabsf(pi.y) + fabsf(pi.z) + fabsf(g.minx) +
+                               fabsf(g.miny) + fabsf(g.minz) + g.cell);
+            slab_dist2(pi.x, g.minx, g.cell, cx, eps, xb2, xa2);
+            slab_dist2(pi.y, g.miny, g.cell, cy, eps, yb2, ya2);
+            slab_dist2(pi.z, g.minz, g.cell, cz, eps, zb2, za2);
+            lim2 = c.k.h2 * 1.0009765625f;
+        }
+    }
+    __device__ __forceinline__ bool range(const int* __restrict__ first, int z, int y, int& s,
+                                          int& e) const {
+        int xa = x0, xb = x1;
+        if (prune) {
+            const float dyz = (z < cz ? zb2 : (z > cz ? za2 : 0.0f)) +
+                              (y < cy ? yb2 : (y > cy ? ya2 : 0.0f));
+            if (dyz > lim2) return false;
+            if (xa < cx && dyz + xb2 > lim2) xa = cx;
+            if (xb > cx && dyz + xa2 > lim2) xb = cx;
+        }
+        const uint32_t row =
+            base + static_cast<uint32_t>(y) * gx + static_cast<uint32_t>(z) * gxy;
+        s = __ldg(&first[row + static_cast<uint32_t>(xa)]);
+        e = __ldg(&first[row + static_cast<uint32_t>(xb) + 1u]);
+        return true;
+    }
+};
+
+// The walk on a group of L lanes (gmask; lane `sub`), for scenes too small
+// to fill the GPU with one thread per particle.  The lanes visit the same
+// rows and chunks together; lane q tests candidates [qW, (q + 1)W) of each
+// 32-candidate chunk (W = 32 / L), the group ORs the hit masks, and each
+// lane writes its own hits at their places in the list (the hits of lower
+// lanes first).  The list is walk()'s, entry for entry; the count is
+// returned on every lane.
 template <bool B, int L>
-__device__ __forceinline__ int walk_split(const StepConst& c, int i, int sub, unsigned gmask,
-                                          float4 pi, const float* __restrict__ sx,
-                                          const float* __restrict__ sy,
-                                          const float* __restrict__ sz,
-                                          const int* __restrict__ first,
-                                          uint32_t* __restrict__ out) {
-    const int P = c.max_nb / L;
+__device__ __forceinline__ int walk_chunks(const StepConst& c, int i, int sub, unsigned gmask,
+                                           float4 pi, const float* __restrict__ sx,
+                                           const float* __restrict__ sy,
+                                           const float* __restrict__ sz,
+                                           const int* __restrict__ first,
+                                           uint32_t* __restrict__ out) {
+    constexpr int W = 32 / L;
+    const StencilRows<B> rows(c, i, pi);
+    const f32x2 h2u = splat2(__uint_as_float(__float_as_uint(c.k.h2) + 1u));
     const size_t stride = nb_step(c);
-    const int mine = walk<B, true, L>(c, i, pi, sx, sy, sz, first,
-                                      out + static_cast<size_t>(sub) * P * stride, P, sub);
-    __syncwarp(gmask);  // every part's stores ordered before any rewrite
-    int incl = mine;
+    const int cap = c.max_nb;
+    const f32x2 px = splat2(pi.x), py = splat2(pi.y), pz = splat2(pi.z);
+    const uint32_t lower = (1u << (sub * W)) - 1u;  // bits of lower lanes' candidates
+    const uint32_t own = W == 32 ? 0xffffffffu : (((1u << W) - 1u) << (sub * W));
+    int count = 0;
+    for (int z = rows.z0; z <= rows.z1; ++z)
+        for (int y = rows.y0; y <= rows.y1; ++y) {
+            int s, e;
+            if (!rows.range(first, z, y, s, e)) continue;
+            for (int j0 = s & ~3; j0 < e; j0 += 32) {
+                const int left = e - j0;
+                const int jb = j0 + sub * W;
+                uint32_t acc = 0u;
+                if (jb < e) {
 #pragma unroll
-    for (int d = 1; d < L; d <<= 1) {
-        const int v = __shfl_up_sync(gmask, incl, d, L);
-        if (sub >= d) incl += v;
-    }
-    const int total = __shfl_sync(gmask, incl, L - 1, L);
-    const bool spill = __any_sync(gmask, mine > P);
-    if (total > c.max_nb) return total;  // overflow: the list is not read
-    if (spill) {
-        if (sub == 0) walk<B>(c, i, pi, sx, sy, sz, first, out, c.max_nb);
-        __syncwarp(gmask);
-        return total;
-    }
-    // Part s's final slots end at or below slot s * P, where part s + 1's
-    // hits start, so moving the parts in order never overwrites hits not yet
-    // moved.
-    const int excl = incl - mine;
+                    for (int q = 0; q < W; q += 4) {
+                        const float4 X = __ldg(reinterpret_cast<const float4*>(sx + jb + q));
+                        const float4 Y = __ldg(reinterpret_cast<const float4*>(sy + jb + q));
+                        const float4 Z = __ldg(reinterpret_cast<const float4*>(sz + jb + q));
+                        const f32x2 da = dist2x2(sub2(px, pack2(X.x, X.y)),
+                                                 sub2(py, pack2(Y.x, Y.y)),
+                                                 sub2(pz, pack2(Z.x, Z.y)));
+                        const f32x2 db = dist2x2(sub2(px, pack2(X.z, X.w)),
+                                                 sub2(py, pack2(Y.z, Y.w)),
+                                                 sub2(pz, pack2(Z.z, Z.w)));
+                        float a0, a1, b0, b1;
+                        unpack2(sub2(da, h2u), a0, a1);
+                        unpack2(sub2(db, h2u), b0, b1);
+                        acc = __funnelshift_l(__float_as_uint(a0), acc, 1);
+                        acc = __funnelshift_l(__float_as_uint(a1), acc, 1);
+                        acc = __funnelshift_l(__float_as_uint(b0), acc, 1);
+                        acc = __funnelshift_l(__float_as_uint(b1), acc, 1);
+                    }
+                }
+                // This lane's W hit bits at its place in the chunk's mask.
+                uint32_t mask = (W == 32 ? __brev(acc) : (__brev(acc) >> (32 - W))) << (sub * W);
 #pragma unroll
-    for (int s = 1; s < L; ++s) {
-        if (sub == s)
-            for (int k = 0; k < mine; ++k)
-                out[static_cast<size_t>(excl + k) * stride] =
-                    out[static_cast<size_t>(s * P + k) * stride];
-        __syncwarp(gmask);
-    }
-    return total;
+                for (int d = 1; d < L; d <<= 1) mask |= __shfl_xor_sync(gmask, mask, d, L);
+                uint32_t valid = left >= 32 ? 0xffffffffu : ((1u << left) - 1u);
+                if (j0 < s) valid &= ~((1u << (s - j0)) - 1u);
+                const int self = i - j0;
+                if (self >= 0 && self < 32) valid &= ~(1u << self);
+                mask &= valid;
+                uint32_t mine = mask & own;
+                int pos = count + __popc(mask & lower);
+                while (mine) {
+                    const int b = __ffs(mine) - 1;
+                    mine &= mine - 1u;
+                    if (pos < cap) out[static_cast<size_t>(pos) * stride] = static_cast<uint32_t>(j0 + b);
+                    ++pos;
+                }
+                count += __popc(mask);
+            }
+        }
+    __syncwarp(gmask);  // the group's stores ordered before any lane reads the list
+    return count;
 }
+
 
 template <int L>
 __device__ __forceinline__ unsigned lane_group_mask() {
@@ -553,10 +616,66 @@ __device__ __forceinline__ unsigned lane_group_mask() {
     return ((1u << L) - 1u) << (lane & ~(L - 1u));
 }
 
-// k_search with L lanes per particle for the walk (slot-major lists only);
-// lane 0 of each group computes lambda.  For scenes too small to fill the
-// GPU with one thread per particle, where a walk is bound by the latency of
-// one thread's row after row.
+// A neighbour sum of particle i spread over its group of L lanes (gmask),
+// the accumulation kept on lane 0 in list order.  In round m, lane q
+// evaluates the V terms of list entry mL + q (term(k, t)), the group hands
+// them to lane 0 by shuffles, and lane 0 adds them in entry order
+// (add(u)).  Each term is the value one lane computes for that entry alone
+// and the additions run in the same order, so the sum is the one-lane
+// loop's, bit for bit; the lanes share the gathers and the term arithmetic.
+template <int L, int V, class Term, class Add>
+__device__ __forceinline__ void group_sum(int count, int sub, unsigned gmask, Term term, Add add) {
+    for (int k0 = 0; k0 < count; k0 += L) {
+        float t[V];
+#pragma unroll
+        for (int v = 0; v < V; ++v) t[v] = 0.0f;
+        if (k0 + sub < count) term(k0 + sub, t);
+#pragma unroll
+        for (int q = 0; q < L; ++q) {
+            float u[V];
+#pragma unroll
+            for (int v = 0; v < V; ++v) u[v] = __shfl_sync(gmask, t[v], q, L);
+            if (sub == 0 && k0 + q < count) add(u);
+        }
+    }
+}
+
+// lambda_of_list on a group of L lanes (the value is lane 0's).
+template <bool B, int L>
+__device__ __forceinline__ float lambda_group(const StepConst& c, int i, int sub, unsigned gmask,
+                                              float4 pi, const float4* __restrict__ xs,
+                                              const uint32_t* __restrict__ out, size_t stride,
+                                              int count) {
+    LambdaAcc acc{c.k.c_poly6, 0.0f, 0.0f, 0.0f, 0.0f};
+    group_sum<L, 4>(
+        count, sub, gmask,
+        [&](int k, float (&t)[4]) {
+            const float4 pj = __ldg(&xs[out[static_cast<size_t>(k) * stride]]);
+            const float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y), dz = fsub(pi.z, pj.z);
+            const float d2 = dist2(dx, dy, dz);
+            t[0] = poly6(c.k, d2);
+            spiky(c.k, dx, dy, dz, d2, t[1], t[2], t[3]);
+        },
+        [&](const float (&u)[4]) {
+            acc.wsum = fadd(acc.wsum, u[0]);
+            acc.s2 = ffma(u[3], u[3], ffma(u[2], u[2], ffma(u[1], u[1], acc.s2)));
+            acc.gx = fadd(acc.gx, u[1]);
+            acc.gy = fadd(acc.gy, u[2]);
+            acc.gz = fadd(acc.gz, u[3]);
+        });
+    if constexpr (B) {
+        const SceneConst& sc = scene_of(c, i);
+        return lambda_finish(sc.mass, sc.rho0, sc.gs2, c.lambda_eps, acc);
+    } else {
+        return lambda_finish(c, acc);
+    }
+}
+
+// k_search with L lanes per particle (slot-major lists only): the group
+// walks the rows together (walk_chunks) and shares lambda's neighbour terms
+// (lambda_group).  For scenes too small to fill the GPU with one thread per
+// particle, where a walk is bound by the latency of one thread's row after
+// row.
 template <bool LAMBDA, bool B, int L>
 __global__ void PBF_WALK_BOUNDS
 k_search_split(const float4* __restrict__ xs, const float* __restrict__ sx,
@@ -570,8 +689,17 @@ k_search_split(const float4* __restrict__ xs, const float* __restrict__ sx,
     if (__any_sync(gmask, fatal(status))) return;
     const float4 pi = xs[i];
     uint32_t* __restrict__ out = nbr + nb_first(c, i);
-    const int count = walk_split<B, L>(c, i, sub, gmask, pi, sx, sy, sz, first, out);
-    if (sub == 0) search_tail<LAMBDA, B>(c, i, pi, xs, out, count, cnt, lam, status);
+    const int count = walk_chunks<B, L>(c, i, sub, gmask, pi, sx, sy, sz, first, out);
+    if (sub == 0) {
+        cnt[i] = count;
+        if (count > c.max_nb) atomicOr(status, kStatusNeighborOverflow);
+    }
+    if (LAMBDA) {
+        const float l = count > c.max_nb
+                            ? CUDART_NAN_F
+                            : lambda_group<B, L>(c, i, sub, gmask, pi, xs, out, nb_step(c), count);
+        if (sub == 0) lam[i] = l;
+    }
 }
 
 // Compact lists, first pass: the walk's neighbour count only.
@@ -806,19 +934,73 @@ __device__ __forceinline__ void delta_sum(const StepConst& c, const float4* __re
     dpz = fmul(gs, az);
 }
 
+// delta_sum with its terms spread over a group of L lanes (lane 0's value).
+template <int N, int L>
+__device__ __forceinline__ void delta_sum_group(const StepConst& c, const float4* __restrict__ xs,
+                                                const uint32_t* __restrict__ nbr,
+                                                const float* __restrict__ lam, int i, int sub,
+                                                unsigned gmask, int count, float4 pi, float gs,
+                                                float& dpx, float& dpy, float& dpz) {
+    const float li = lam[i];
+    const uint32_t* row = nbr + nb_first(c, i);
+    const size_t st = nb_step(c);
+    float ax = 0.0f, ay = 0.0f, az = 0.0f;
+    group_sum<L, 4>(
+        count, sub, gmask,
+        [&](int k, float (&t)[4]) {
+            const uint32_t j = __ldg(&row[static_cast<size_t>(k) * st]);
+            const float4 pj = __ldg(&xs[j]);
+            const float lj = __ldg(&lam[j]);
+            const float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y), dz = fsub(pi.z, pj.z);
+            const float d2 = dist2(dx, dy, dz);
+            spiky(c.k, dx, dy, dz, d2, t[1], t[2], t[3]);
+            t[0] = fadd(fadd(li, lj), scorr<N>(c.sc, d2));
+        },
+        [&](const float (&u)[4]) {
+            ax = ffma(u[0], u[1], ax);
+            ay = ffma(u[0], u[2], ay);
+            az = ffma(u[0], u[3], az);
+        });
+    dpx = fmul(gs, ax);
+    dpy = fmul(gs, ay);
+    dpz = fmul(gs, az);
+}
+
+// The thread's particle and lane in a launch of L lanes per particle; false
+// for threads past the last particle (whole groups) and, group-wide, once a
+// fatal status bit is set.
+template <int L>
+__device__ __forceinline__ bool group_thread(int n, const unsigned* status, int& i, int& sub,
+                                             unsigned& gmask) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    i = t / L;
+    sub = t % L;
+    gmask = 0u;
+    if (i >= n) return false;
+    if constexpr (L == 1) {
+        return !fatal(status);
+    } else {
+        gmask = lane_group_mask<L>();
+        return !__any_sync(gmask, fatal(status));
+    }
+}
+
 // delta p + applyDeltaPosition + CollisionSystem::solve + next cell keys.
 // N: artificial-pressure exponent fixed at compile time (0 = read at run time).
 // moved (optional): bit a set where the projection changed component a.
 // pre (optional): the position before the projection.
-template <int N, bool B>
+// L lanes per particle share the neighbour terms (small scenes, with the
+// split walks); lane 0 applies.
+template <int N, bool B, int L>
 __global__ void PBF_GATHER_REGS(48)
 k_delta_apply(const float4* __restrict__ xs, const uint32_t* __restrict__ nbr,
               const int* __restrict__ cnt, const float* __restrict__ lam, StepConst c, int n,
               float4* __restrict__ xs_out, uint32_t* __restrict__ keys_out,
               uint8_t* __restrict__ moved, float4* __restrict__ pre,
               unsigned* __restrict__ status) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n || fatal(status)) return;
+    int i, sub;
+    unsigned gmask;
+    if (!group_thread<L>(n, status, i, sub, gmask)) return;
     const float4 pi = xs[i];
     const int count = cnt[i];
     float dpx, dpy, dpz;
@@ -826,8 +1008,12 @@ k_delta_apply(const float4* __restrict__ xs, const uint32_t* __restrict__ nbr,
         dpx = dpy = dpz = CUDART_NAN_F;
     } else {
         const float gs = B ? scene_of(c, i).gs : c.gs;
-        delta_sum<N>(c, xs, nbr, lam, i, count, pi, gs, dpx, dpy, dpz);
+        if constexpr (L == 1)
+            delta_sum<N>(c, xs, nbr, lam, i, count, pi, gs, dpx, dpy, dpz);
+        else
+            delta_sum_group<N, L>(c, xs, nbr, lam, i, sub, gmask, count, pi, gs, dpx, dpy, dpz);
     }
+    if (sub != 0) return;
     float px = fadd(pi.x, dpx), py = fadd(pi.y, dpy), pz = fadd(pi.z, dpz);
     const float ux = px, uy = py, uz = pz;
     if (pre) pre[i] = make_float4(ux, uy, uz, pi.w);
@@ -956,8 +1142,8 @@ k_search_xsph(const float4* __restrict__ xs, const float* __restrict__ sx,
     xsph_tail<B>(c, i, pi, xs, nbr, count, cnt, v, v_out, vin, resolve, status);
 }
 
-// k_search_xsph with L lanes per particle for the walk; lane 0 of each group
-// applies XSPH (see k_search_split).
+// k_search_xsph with L lanes per particle: the group walks together
+// (walk_chunks) and shares the XSPH terms; lane 0 writes.
 template <bool B, int L>
 __global__ void PBF_WALK_BOUNDS
 k_search_xsph_split(const float4* __restrict__ xs, const float* __restrict__ sx,
@@ -973,8 +1159,43 @@ k_search_xsph_split(const float4* __restrict__ xs, const float* __restrict__ sx,
     if (__any_sync(gmask, fatal(status))) return;
     const float4 pi = xs[i];
     const int count =
-        walk_split<B, L>(c, i, sub, gmask, pi, sx, sy, sz, first, nbr + nb_first(c, i));
-    if (sub == 0) xsph_tail<B>(c, i, pi, xs, nbr, count, cnt, v, v_out, vin, resolve, status);
+        walk_chunks<B, L>(c, i, sub, gmask, pi, sx, sy, sz, first, nbr + nb_first(c, i));
+    if (sub == 0) {
+        cnt[i] = count;
+        if (count > c.max_nb) atomicOr(status, kStatusNeighborOverflow);
+    }
+    // applyXsphViscosity over the new list, its terms spread over the group.
+    const float4 vi = v[i];
+    float4 out;
+    if (!count_ok(count, c.max_nb)) {
+        out = make_float4(CUDART_NAN_F, CUDART_NAN_F, CUDART_NAN_F, vi.w);
+    } else {
+        const uint32_t* row = nbr + nb_first(c, i);
+        const size_t st = nb_step(c);
+        float cx = 0.0f, cy = 0.0f, cz = 0.0f;
+        group_sum<L, 4>(
+            count, sub, gmask,
+            [&](int k, float (&t)[4]) {
+                const uint32_t j = row[static_cast<size_t>(k) * st];  // written above
+                const float4 pj = __ldg(&xs[j]), vj = __ldg(&v[j]);
+                t[0] = poly6(c.k, dist2(fsub(pi.x, pj.x), fsub(pi.y, pj.y), fsub(pi.z, pj.z)));
+                t[1] = fsub(vj.x, vi.x);
+                t[2] = fsub(vj.y, vi.y);
+                t[3] = fsub(vj.z, vi.z);
+            },
+            [&](const float (&u)[4]) {
+                cx = ffma(u[1], u[0], cx);
+                cy = ffma(u[2], u[0], cy);
+                cz = ffma(u[3], u[0], cz);
+            });
+        const float xc = B ? scene_of(c, i).xsph_c : c.xsph_c;
+        out = make_float4(ffma(xc, cx, vi.x), ffma(xc, cy, vi.y), ffma(xc, cz, vi.z), vi.w);
+    }
+    if (sub != 0) return;
+    if (resolve)
+        resolve_velocity(colliders_of<B>(c, i), c.particle_radius, c.restitution, c.friction, pi,
+                         vin[i], out);
+    v_out[i] = out;
 }
 
 // computeVorticity (pbf_solver_kernels.cu:268-315).
@@ -1033,6 +1254,22 @@ __global__ void __launch_bounds__(kBlock) k_omega_norm(float4* __restrict__ om, 
     om[i] = w;
 }
 
+// The confinement velocity from the summed eta = sum (|w_j| - |w_i|) grad W.
+__device__ __forceinline__ float4 confine_finish(const StepConst& c, float ex, float ey, float ez,
+                                                 float4 wi, float4 vi) {
+    const float el = len3(ex, ey, ez);
+    float nx = 0.0f, ny = 0.0f, nz = 0.0f;
+    if (el > kEtaEpsilon) {
+        nx = fdiv(ex, el);
+        ny = fdiv(ey, el);
+        nz = fdiv(ez, el);
+    }
+    const float cx = fmul(c.vort_eps, crossc(ny, nz, wi.y, wi.z));
+    const float cy = fmul(c.vort_eps, crossc(nz, nx, wi.z, wi.x));
+    const float cz = fmul(c.vort_eps, crossc(nx, ny, wi.x, wi.y));
+    return make_float4(ffma(c.dt, cx, vi.x), ffma(c.dt, cy, vi.y), ffma(c.dt, cz, vi.z), vi.w);
+}
+
 // applyVorticityConfinement (pbf_solver_kernels.cu:317-385).
 __device__ __forceinline__ float4 confine_one(const StepConst& c, const float4* __restrict__ x,
                                               const uint32_t* __restrict__ nbr, int count,
@@ -1070,17 +1307,7 @@ __device__ __forceinline__ float4 confine_one(const StepConst& c, const float4* 
             ey = ffma(md, gy, ey);
             ez = ffma(md, gz, ez);
         });
-    const float el = len3(ex, ey, ez);
-    float nx = 0.0f, ny = 0.0f, nz = 0.0f;
-    if (el > kEtaEpsilon) {
-        nx = fdiv(ex, el);
-        ny = fdiv(ey, el);
-        nz = fdiv(ez, el);
-    }
-    const float cx = fmul(c.vort_eps, crossc(ny, nz, wi.y, wi.z));
-    const float cy = fmul(c.vort_eps, crossc(nz, nx, wi.z, wi.x));
-    const float cz = fmul(c.vort_eps, crossc(nx, ny, wi.x, wi.y));
-    return make_float4(ffma(c.dt, cx, vi.x), ffma(c.dt, cy, vi.y), ffma(c.dt, cz, vi.z), vi.w);
+    return confine_finish(c, ex, ey, ez, wi, vi);
 }
 
 template <bool B>
@@ -1096,6 +1323,49 @@ k_confine(const float4* __restrict__ x, const uint32_t* __restrict__ nbr,
         resolve_velocity(colliders_of<B>(c, i), c.particle_radius, c.restitution, c.friction,
                          x[i], vin[i], out);
     v_out[i] = out;
+}
+
+// k_vorticity with L lanes per particle sharing the neighbour terms (small
+// scenes); lane 0 writes.
+template <int L>
+__global__ void __launch_bounds__(kMaxTunedBlock)
+k_vorticity_group(const float4* __restrict__ x, const float4* __restrict__ v,
+                  const uint32_t* __restrict__ nbr, const int* __restrict__ cnt, StepConst c,
+                  int n, float4* __restrict__ omega, bool store_norm,
+                  const unsigned* __restrict__ status) {
+    int i, sub;
+    unsigned gmask;
+    if (!group_thread<L>(n, status, i, sub, gmask)) return;
+    const int count = cnt[i];
+    if (!count_ok(count, c.max_nb)) {
+        if (sub == 0)
+            omega[i] = make_float4(CUDART_NAN_F, CUDART_NAN_F, CUDART_NAN_F,
+                                   store_norm ? CUDART_NAN_F : 0.0f);
+        return;
+    }
+    const float4 pi = x[i], vi = v[i];
+    const uint32_t* row = nbr + nb_first(c, i);
+    const size_t st = nb_step(c);
+    float ox = 0.0f, oy = 0.0f, oz = 0.0f;
+    group_sum<L, 3>(
+        count, sub, gmask,
+        [&](int k, float (&t)[3]) {
+            const uint32_t j = __ldg(&row[static_cast<size_t>(k) * st]);
+            const float4 pj = __ldg(&x[j]), vj = __ldg(&v[j]);
+            const float dx = fsub(pi.x, pj.x), dy = fsub(pi.y, pj.y), dz = fsub(pi.z, pj.z);
+            float gx, gy, gz;
+            spiky(c.k, dx, dy, dz, dist2(dx, dy, dz), gx, gy, gz);
+            const float vx = fsub(vj.x, vi.x), vy = fsub(vj.y, vi.y), vz = fsub(vj.z, vi.z);
+            t[0] = crossc(gy, gz, vy, vz);
+            t[1] = crossc(gz, gx, vz, vx);
+            t[2] = crossc(gx, gy, vx, vy);
+        },
+        [&](const float (&u)[3]) {
+            ox = fadd(ox, u[0]);
+            oy = fadd(oy, u[1]);
+            oz = fadd(oz, u[2]);
+        });
+    if (sub == 0) omega[i] = make_float4(ox, oy, oz, store_norm ? len3(ox, oy, oz) : 0.0f);
 }
 
 template <bool B>
@@ -1248,11 +1518,10 @@ void launch_gather_first(const uint32_t* perm, const float4* xs_in, float4* xs_o
 }
 inline int tuned_block(const StepConst& c, int k) { return c.blk[k] > 0 ? c.blk[k] : kBlock; }
 
-// Scene size below which the walks split each particle's rows over 4 lanes
-// by default.  Measured per walk + lambda launch (1 / 2 / 4 lanes): 43.5 /
-// 36.9 / 35.7 us at 16,384 particles, 40.2 / 45.8 / 61.4 us at 65,536 (from
-// there on lane 0's lambda pass, alone in its group, costs more than the
-// split walk saves).
+// Scene size below which a group of 4 lanes walks each particle by default.
+// Measured steps of the dam break at 1 / 2 / 4 lanes: 0.280 / 0.329 / 0.248 ms
+// at 16,384 particles, 0.257 / 0.343 / 0.286 at 32,768, 0.316 / 0.399 / 0.424 at
+// 65,536 (from there on the GPU is full with one lane per particle).
 constexpr size_t kSplitWalk4Below = size_t(1) << 15;
 
 // Lanes per particle of a launch: c.walk_lanes where the split walk applies.
@@ -1379,9 +1648,18 @@ void launch_delta_apply_b(const float4* xs, const uint32_t* nbr, const int* cnt,
                           uint8_t* moved, float4* pre, unsigned* status, cudaStream_t st) {
     const int bs = tuned_block(c, kTunedDelta);
     const unsigned g = blocks_for(n, bs);
+    const int L = split_lanes(c, n);
+    const unsigned gl = blocks_for(static_cast<size_t>(n) * L, bs);
 #define PBF_DELTA_CASE(N)                                                                        \
-    launch_k(k_delta_apply<N, B>, g, bs, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out, moved,   \
-             pre, status)
+    if (L == 4)                                                                                  \
+        launch_k(k_delta_apply<N, B, 4>, gl, bs, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out,  \
+                 moved, pre, status);                                                            \
+    else if (L == 2)                                                                             \
+        launch_k(k_delta_apply<N, B, 2>, gl, bs, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out,  \
+                 moved, pre, status);                                                            \
+    else                                                                                         \
+        launch_k(k_delta_apply<N, B, 1>, g, bs, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out,   \
+                 moved, pre, status)
     switch (c.sc.k != 0.0f ? c.sc.n : 0) {
         case 1: PBF_DELTA_CASE(1); break;
         case 2: PBF_DELTA_CASE(2); break;
@@ -1423,8 +1701,17 @@ void launch_vorticity(const float4* x, const float4* v, const uint32_t* nbr, con
                       const StepConst& c, int n, float4* omega, bool store_norm,
                       const unsigned* status, cudaStream_t st) {
     const int bs = tuned_block(c, kTunedVorticity);
-    launch_k(k_vorticity, blocks_for(n, bs), bs, st, x, v, nbr, cnt, c, n, omega, store_norm,
-             status);
+    const int L = split_lanes(c, n);
+    const unsigned gl = blocks_for(static_cast<size_t>(n) * L, bs);
+    if (L == 4)
+        launch_k(k_vorticity_group<4>, gl, bs, st, x, v, nbr, cnt, c, n, omega, store_norm,
+                 status);
+    else if (L == 2)
+        launch_k(k_vorticity_group<2>, gl, bs, st, x, v, nbr, cnt, c, n, omega, store_norm,
+                 status);
+    else
+        launch_k(k_vorticity, blocks_for(n, bs), bs, st, x, v, nbr, cnt, c, n, omega, store_norm,
+                 status);
 }
 void launch_omega_norm(float4* omega, int n, cudaStream_t st) {
     launch_k(k_omega_norm, blocks_for(n), kBlock, st, omega, n);

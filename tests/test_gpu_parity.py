@@ -203,12 +203,12 @@ def test_neighbor_lists_bit_exact_vs_oracle_slot_order(pbf, scenes, orc):
         assert_bitwise(nb[k * n:(k + 1) * n][used], onb[k * n:(k + 1) * n][used], "slot %d" % k)
 
 
-def test_split_walk_part_overflow_falls_back(pbf, scenes, orc):
-    """Small scenes split each particle's stencil rows over lanes, each part
-    writing into its share of the list slots; when all neighbours lie in one
-    row (a line of particles along x) one part overflows its share while the
-    whole list fits, and the particle is walked again in one lane.  The
-    result is the one-lane result, bit for bit."""
+def test_group_walk_line_of_particles(pbf, scenes, orc):
+    """Small scenes walk each particle's stencil on a group of four lanes,
+    each lane testing its quarter of every 32-candidate chunk and writing its
+    own hits in list order.  A line of particles along x puts every
+    neighbour in one row, so one chunk holds hits of several lanes; the
+    lists, counts and the whole step are the one-lane result, bit for bit."""
     k = 200
     pos = np.ones((k, 4), np.float32)
     pos[:, 0] = np.float32(0.05) + np.arange(k, dtype=np.float32) * np.float32(0.02)
@@ -224,5 +224,6 @@ def test_split_walk_part_overflow_falls_back(pbf, scenes, orc):
     assert_bitwise(s.copy_velocities_to_host(), o.velocities(), "velocities")
     wp, wid, wcnt = s.working_state()
     op, oid, ocnt = o.working()
-    assert wcnt.max() > 32 // 4, "the scene must overflow one part's share of slots"
+    assert s.walk_lanes() == 4
+    assert wcnt.max() > 8, "hits must span several lanes' quarters of a chunk"
     assert_bitwise(wcnt, ocnt, "neighbour counts")
