@@ -13,8 +13,14 @@
 //             + per-warp running counters, items visited in index order),
 //             tile staged in shared memory in digit order, then written out
 //             as contiguous runs (coalesced stores)
-// No kernel waits on another block, so nothing can spin.
+// Up to 16,384 keys one thread-block cluster does every pass in a single
+// launch (k_sort_cluster: the keys stay in the CTAs' shared memory and move
+// between them through distributed shared memory, with cluster barriers).
+// No kernel spins on another block: the cluster barrier is the hardware's,
+// and every CTA of a cluster is resident together.
 #include "pbf_kernels.cuh"
+
+#include <cooperative_groups.h>
 
 #include <algorithm>
 
@@ -244,6 +250,125 @@ k_downsweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ v
     }
 }
 
+// ---------------------------------------------------------------------------
+// Sorts of up to kClusterSortMax keys: one cluster of kClusterCtas CTAs (the
+// portable cluster size) does every pass in one launch.  CTA r holds sorted
+// positions [r kCTile, (r + 1) kCTile) of the current pass in shared
+// memory.  A pass ranks the CTA's keys by digit (warp match + per-warp
+// counters, items in position order: stable), reads every CTA's digit
+// histogram through distributed shared memory to place its runs, and
+// writes each key straight into the shared memory of the CTA that holds its
+// destination.  Two cluster barriers a pass: the histograms complete before
+// any is read, and every key delivered (and every histogram read) before
+// the next pass.  The last pass's CTAs write their slices out.  The result
+// is the multi-launch sort's: stable by digit, earlier positions first.
+// ---------------------------------------------------------------------------
+namespace cg = cooperative_groups;
+constexpr int kCThreads = 512, kCItems = 4, kCWarps = kCThreads / 32;
+constexpr int kCTile = kCThreads * kCItems;  // 2,048 keys per CTA
+constexpr int kClusterCtas = 8;
+constexpr int kClusterSortMax = kCTile * kClusterCtas;
+constexpr int kCWarpChunk = kCTile / kCWarps;  // 128 consecutive positions per warp
+
+__global__ void __cluster_dims__(kClusterCtas, 1, 1) __launch_bounds__(kCThreads)
+k_sort_cluster(const uint32_t* __restrict__ keys, uint32_t* __restrict__ sorted_keys,
+               uint32_t* __restrict__ sorted_idx, int n, int passes, int bits_per_pass) {
+    __shared__ uint32_t buf_k[2][kCTile], buf_v[2][kCTile];
+    __shared__ uint16_t wcnt[kCWarps][kMaxBins];  // per-warp digit counts (<= 128 each)
+    __shared__ uint32_t hist[kMaxBins];            // this CTA's digit counts
+    __shared__ uint32_t run_off[kMaxBins];         // global start of this CTA's digit run
+    __shared__ uint32_t warp_sums[kCWarps];
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = static_cast<int>(cluster.block_rank());
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t lt_mask = (1u << lane) - 1u;
+    const uint32_t mask = (1u << bits_per_pass) - 1u;
+    const int bins = static_cast<int>(mask) + 1;
+    int cur = 0;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = p * bits_per_pass;
+        uint32_t k_reg[kCItems], v_reg[kCItems], r_reg[kCItems];
+#pragma unroll
+        for (int r = 0; r < kCItems; ++r) {
+            const int idx = warp * kCWarpChunk + r * 32 + lane;  // slot in the CTA
+            const int pos = rank * kCTile + idx;
+            if (pos < n) {
+                k_reg[r] = p == 0 ? keys[pos] : buf_k[cur][idx];
+                v_reg[r] = p == 0 ? static_cast<uint32_t>(pos) : buf_v[cur][idx];
+            } else {
+                k_reg[r] = 0u;
+                v_reg[r] = 0u;
+            }
+        }
+        for (int d = tid; d < bins; d += kCThreads) {
+#pragma unroll
+            for (int w = 0; w < kCWarps; ++w) wcnt[w][d] = 0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < kCItems; ++r) {
+            const int pos = rank * kCTile + warp * kCWarpChunk + r * 32 + lane;
+            const bool valid = pos < n;
+            const uint32_t digit = valid ? (k_reg[r] >> shift) & mask : 0xffffffffu;
+            const uint32_t peers = __match_any_sync(0xffffffffu, digit);
+            const int leader = __ffs(peers) - 1;
+            uint32_t prior = 0;
+            if (valid && lane == leader) {
+                prior = wcnt[warp][digit];
+                wcnt[warp][digit] = static_cast<uint16_t>(prior + __popc(peers));
+            }
+            prior = __shfl_sync(0xffffffffu, prior, leader);
+            r_reg[r] = valid ? prior + __popc(peers & lt_mask) : 0xffffffffu;
+            __syncwarp();
+        }
+        __syncthreads();
+        // Per digit: exclusive scan over the warps (earlier warps hold
+        // earlier positions) and the CTA's count.
+        if (tid < bins) {
+            uint32_t run = 0;
+#pragma unroll
+            for (int w = 0; w < kCWarps; ++w) {
+                const uint32_t c = wcnt[w][tid];
+                wcnt[w][tid] = static_cast<uint16_t>(run);
+                run += c;
+            }
+            hist[tid] = run;
+        }
+        cluster.sync();  // every CTA's histogram complete
+        {
+            uint32_t total = 0u, before = 0u;
+            if (tid < bins) {
+                for (int q = 0; q < kClusterCtas; ++q) {
+                    const uint32_t h = *cluster.map_shared_rank(&hist[tid], q);
+                    total += h;
+                    before += q < rank ? h : 0u;
+                }
+            }
+            uint32_t all;
+            const uint32_t dbase = block_exclusive_scan<kCWarps>(total, warp_sums, all);
+            if (tid < bins) run_off[tid] = dbase + before;
+        }
+        __syncthreads();
+        const int nxt = cur ^ 1;
+#pragma unroll
+        for (int r = 0; r < kCItems; ++r) {
+            if (r_reg[r] == 0xffffffffu) continue;
+            const uint32_t digit = (k_reg[r] >> shift) & mask;
+            const uint32_t dst = run_off[digit] + wcnt[warp][digit] + r_reg[r];
+            const int q = static_cast<int>(dst / kCTile), slot = static_cast<int>(dst % kCTile);
+            *cluster.map_shared_rank(&buf_k[nxt][slot], q) = k_reg[r];
+            *cluster.map_shared_rank(&buf_v[nxt][slot], q) = v_reg[r];
+        }
+        cluster.sync();  // every key delivered and every histogram read
+        cur = nxt;
+    }
+    const int count = min(kCTile, n - rank * kCTile);
+    for (int k = tid; k < count; k += kCThreads) {
+        sorted_keys[rank * kCTile + k] = buf_k[cur][k];
+        sorted_idx[rank * kCTile + k] = buf_v[cur][k];
+    }
+}
+
 }  // namespace
 
 SortPlan make_sort_plan(int n, uint64_t num_cells, int tile) {
@@ -269,6 +394,7 @@ size_t sort_scratch_bytes(int max_n) {
 }
 
 int sort_kernel_count(const SortPlan& plan) {
+    if (plan.n <= kClusterSortMax) return 1;
     return plan.passes * (plan.tiles <= kSumTilesMax ? 2 : 3);
 }
 
@@ -304,6 +430,13 @@ void sort_passes(const SortPlan& plan, const uint32_t* keys, uint32_t* sorted_ke
 void launch_sort(const SortPlan& plan, const uint32_t* keys, uint32_t* sorted_keys,
                  uint32_t* sorted_idx, uint32_t* alt_keys, uint32_t* alt_idx, void* scratch,
                  const unsigned* status, cudaStream_t st) {
+    if (plan.n <= kClusterSortMax) {
+        // Nothing to sort is sorted: zero keys launch nothing.
+        if (plan.n > 0)
+            launch_k(k_sort_cluster, static_cast<unsigned>(kClusterCtas), kCThreads, st, keys,
+                     sorted_keys, sorted_idx, plan.n, plan.passes, plan.bits_per_pass);
+        return;
+    }
     if (plan.tile == Small::kTile)
         sort_passes<Small>(plan, keys, sorted_keys, sorted_idx, alt_keys, alt_idx, scratch, status,
                            st);

@@ -89,10 +89,12 @@ def test_batch_takes_exactly_all_particles(pbf, scenes):
 
 def test_batch_one_launch_per_stage(pbf, scenes):
     """A frame's kernel count does not grow with the number of scenes: one
-    launch per stage covers them all (both batches sort in two passes)."""
+    launch per stage covers them all.  8 and 20 scenes, 24,844 and 26,508
+    particles: both sort in two passes of 25-26 tiles (the sort's launch
+    count depends on the key count and bits, not on the scenes)."""
     counts = []
-    for k in (5, 20):
-        sc, prm, pos, vel, _ = scenes.batched_scenes(n_scenes=k, n_min=512, n_max=2048, seed=4)
+    for k, lo, hi in ((8, 2048, 4096), (20, 512, 2048)):
+        sc, prm, pos, vel, _ = scenes.batched_scenes(n_scenes=k, n_min=lo, n_max=hi, seed=4)
         b = pbf.PBFSolver()
         b.initialize_batch(sc, prm)
         b.set_particles(pos, vel)
