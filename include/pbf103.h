@@ -174,9 +174,9 @@ pbf_status pbf_sort_tile(const pbf_solver* s, int* keys_per_tile);
  * compact lists; at most max_neighbors). */
 pbf_status pbf_walk_lanes(const pbf_solver* s, int* lanes);
 /* Sets the lanes per particle of the walks: 1, 2 or 4, or 0 for the default
- * by scene size.  Results do not change.  The split pays when one small scene
- * leaves the GPU idle; many small solvers running at once on separate streams
- * step faster with 1 (256 scenes: 11.3 against 18.4 ms per step). */
+ * by scene size.  Results do not change.  A lane group pays when one small
+ * scene leaves the GPU idle; many small solvers running at once on separate
+ * streams fill it already and step faster with 1. */
 pbf_status pbf_set_walk_lanes(pbf_solver* s, int lanes);
 
 /* ---- reverse-mode derivative (no counterpart in the reference) ---------
