@@ -39,15 +39,6 @@ void launch_error_check(cudaError_t e) { cuda_check(e); }
 // spills, 6 % faster at 1M particles).
 #define PBF_GATHER_REGS(r) __maxnreg__(r)
 
-// Register budget of the list-writing walks (k_search, k_count,
-// k_search_xsph and their split forms): the 16-candidate test keeps twelve
-// 16-byte loads in flight, so the walk trades registers against resident
-// warps.  PBF_WALK_REGS (a build flag) caps it for measurements.
-#ifdef PBF_WALK_REGS
-#define PBF_WALK_BOUNDS __maxnreg__(PBF_WALK_REGS)
-#else
-#define PBF_WALK_BOUNDS __launch_bounds__(kMaxTunedBlock)
-#endif
 
 namespace {
 
@@ -289,24 +280,87 @@ __device__ __forceinline__ void slab_dist2(float p, float lo, float cell, int k,
 // The neighbour walk of particle i (position pi): writes the list slot-major
 // at out[slot * stride] (at most cap entries) and returns the full count.
 // STORE = false counts the hits without writing the list.
+// The stencil rows of particle i, as the walks visit them: z0..z1 x y0..y1
+// (clamped to the grid), and range(z, y) gives row (z, y)'s candidate index
+// range [s, e): its cells x0..x1 are consecutive keys.  Keys fit in 32 bits
+// (cells < 2^32 is checked at initialisation), so the reference's 64-bit key
+// arithmetic truncates to the same values.
+// Cell pruning (radius 1): a stencil cell whose box lies farther than h
+// from the particle holds no neighbour, so range() returns false for the
+// rows (y, z) that far and leaves out the end cells of a row that far.  Per
+// axis, eps = 2^-14 (|p| + |min| + cell) covers the FP32 rounding of every
+// cell index (floor((p - min) / cell)) and of the candidates' differences,
+// and the bound h2 (1 + 2^-10) the rounding of d2: only certain misses are
+// left out, so the list is entry for entry the unpruned walk's.
+template <bool B>
+struct StencilRows {
+    GridConst g;
+    uint32_t base, gx, gxy;
+    int cx, cy, cz, x0, x1, y0, y1, z0, z1;
+    bool prune;
+    float xb2, xa2, yb2, ya2, zb2, za2, lim2;
+    __device__ __forceinline__ StencilRows(const StepConst& c, int i, float4 pi) {
+        grid_of<B>(c, i, g, base);
+        cell_of(g, pi.x, pi.y, pi.z, cx, cy, cz);
+        const int R = g.radius;
+        x0 = max(0, cx - R);
+        x1 = min(g.gx - 1, cx + R);
+        y0 = max(0, cy - R);
+        y1 = min(g.gy - 1, cy + R);
+        z0 = max(0, cz - R);
+        z1 = min(g.gz - 1, cz + R);
+        gx = static_cast<uint32_t>(g.gx);
+        gxy = gx * static_cast<uint32_t>(g.gy);
+        prune = c.prune_cells && R == 1;
+        xb2 = xa2 = yb2 = ya2 = zb2 = za2 = lim2 = 0.0f;
+        if (prune) {
+            const float eps = 6.103515625e-05f *
+                              (fabsf(pi.x) + fabsf(pi.y) + fabsf(pi.z) + fabsf(g.minx) +
+                               fabsf(g.miny) + fabsf(g.minz) + g.cell);
+            slab_dist2(pi.x, g.minx, g.cell, cx, eps, xb2, xa2);
+            slab_dist2(pi.y, g.miny, g.cell, cy, eps, yb2, ya2);
+            slab_dist2(pi.z, g.minz, g.cell, cz, eps, zb2, za2);
+            lim2 = c.k.h2 * 1.0009765625f;
+        }
+    }
+    __device__ __forceinline__ bool range(const int* __restrict__ first, int z, int y, int& s,
+                                          int& e) const {
+        int xa = x0, xb = x1;
+        if (prune) {
+            const float dyz = (z < cz ? zb2 : (z > cz ? za2 : 0.0f)) +
+                              (y < cy ? yb2 : (y > cy ? ya2 : 0.0f));
+            if (dyz > lim2) return false;
+            if (xa < cx && dyz + xb2 > lim2) xa = cx;
+            if (xb > cx && dyz + xa2 > lim2) xb = cx;
+        }
+        const uint32_t row =
+            base + static_cast<uint32_t>(y) * gx + static_cast<uint32_t>(z) * gxy;
+        s = __ldg(&first[row + static_cast<uint32_t>(xa)]);
+        e = __ldg(&first[row + static_cast<uint32_t>(xb) + 1u]);
+        return true;
+    }
+};
+
+// Bits of a 32-candidate chunk from j0 that belong to the row range [s, e),
+// less the particle i itself.
+__device__ __forceinline__ uint32_t chunk_valid(int j0, int s, int e, int i) {
+    const int left = e - j0;
+    uint32_t valid = left >= 32 ? 0xffffffffu : ((1u << left) - 1u);
+    if (j0 < s) valid &= ~((1u << (s - j0)) - 1u);
+    const int self = i - j0;
+    if (self >= 0 && self < 32) valid &= ~(1u << self);
+    return valid;
+}
+
+// The neighbour walk of particle i (position pi): writes the list slot-major
+// at out[slot * stride] (at most cap entries) and returns the full count.
+// STORE = false counts the hits without writing the list.
 template <bool B, bool STORE = true>
 __device__ __forceinline__ int walk(const StepConst& c, int i, float4 pi,
                                     const float* __restrict__ sx, const float* __restrict__ sy,
                                     const float* __restrict__ sz, const int* __restrict__ first,
                                     uint32_t* __restrict__ out, int cap) {
-    GridConst g;
-    uint32_t base;
-    grid_of<B>(c, i, g, base);
-    int cx, cy, cz;
-    cell_of(g, pi.x, pi.y, pi.z, cx, cy, cz);
-    const int R = g.radius;
-    const int x0 = max(0, cx - R), x1 = min(g.gx - 1, cx + R);
-    const int y0 = max(0, cy - R), y1 = min(g.gy - 1, cy + R);
-    const int z0 = max(0, cz - R), z1 = min(g.gz - 1, cz + R);
-    // Keys fit in 32 bits (cells < 2^32 is checked at initialisation), so
-    // the reference's 64-bit key arithmetic truncates to the same values.
-    const uint32_t gx = static_cast<uint32_t>(g.gx);
-    const uint32_t gxy = gx * static_cast<uint32_t>(g.gy);
+    const StencilRows<B> rows(c, i, pi);
     // The hit test d2 <= h2 as a sign bit: for finite d2 it holds exactly
     // when d2 - h2u < 0, h2u being the float just above h2 (the difference
     // of two distinct floats is never zero, and +inf or NaN, the canonical
@@ -314,24 +368,6 @@ __device__ __forceinline__ int walk(const StepConst& c, int i, float4 pi,
     const f32x2 h2u = splat2(__uint_as_float(__float_as_uint(c.k.h2) + 1u));
     const size_t stride = nb_step(c);
     const f32x2 px = splat2(pi.x), py = splat2(pi.y), pz = splat2(pi.z);
-    // Cell pruning (radius 1): a stencil cell whose box lies farther than h
-    // from the particle holds no neighbour, so the rows (y, z) and the end
-    // cells of a row that are that far are not read.  Per axis, eps =
-    // 2^-14 (|p| + |min| + cell) covers the FP32 rounding of every cell
-    // index (floor((p - min) / cell)) and of the candidates' differences,
-    // and the bound h2 (1 + 2^-10) the rounding of d2: only certain misses
-    // are left out, so the list is entry for entry the unpruned walk's.
-    const bool prune = c.prune_cells && R == 1;
-    float xb2 = 0.0f, xa2 = 0.0f, yb2 = 0.0f, ya2 = 0.0f, zb2 = 0.0f, za2 = 0.0f, lim2 = 0.0f;
-    if (prune) {
-        const float eps = 6.103515625e-05f *
-                          (fabsf(pi.x) + fabsf(pi.y) + fabsf(pi.z) + fabsf(g.minx) +
-                           fabsf(g.miny) + fabsf(g.minz) + g.cell);
-        slab_dist2(pi.x, g.minx, g.cell, cx, eps, xb2, xa2);
-        slab_dist2(pi.y, g.miny, g.cell, cy, eps, yb2, ya2);
-        slab_dist2(pi.z, g.minz, g.cell, cz, eps, zb2, za2);
-        lim2 = c.k.h2 * 1.0009765625f;
-    }
     int count = 0;
     // 16 candidates from j (a multiple of 4): the x, y, z arrays are read
     // four floats at a time and tested two at a time with FP32x2
@@ -356,56 +392,37 @@ __device__ __forceinline__ int walk(const StepConst& c, int i, float4 pi,
             acc = __funnelshift_l(__float_as_uint(b1), acc, 1);
         }
     };
-    // Rows z -> y; inside a row the cells xa..xb are consecutive keys, so the
-    // candidates of the row are one index range walked in ascending order --
-    // exactly the reference's z -> y -> x cell walk (neighbors.cu:52-86).
-    // Each range is tested in 32-candidate chunks from a multiple of 4 (the
-    // second half of a chunk only if the range reaches it); candidates
-    // outside [s, e) and the particle itself are masked off, and the hits
-    // are then appended in ascending order.  The component arrays are padded
-    // (soa_stride_for), so a chunk may read past the last particle.
-    auto row_walk = [&](int z, int y) {
-        int xa = x0, xb = x1;
-        if (prune) {
-            const float dyz = (z < cz ? zb2 : (z > cz ? za2 : 0.0f)) +
-                              (y < cy ? yb2 : (y > cy ? ya2 : 0.0f));
-            if (dyz > lim2) return;
-            if (xa < cx && dyz + xb2 > lim2) xa = cx;
-            if (xb > cx && dyz + xa2 > lim2) xb = cx;
-        }
-        const uint32_t row =
-            base + static_cast<uint32_t>(y) * gx + static_cast<uint32_t>(z) * gxy;
-        const int s = __ldg(&first[row + static_cast<uint32_t>(xa)]);
-        const int e = __ldg(&first[row + static_cast<uint32_t>(xb) + 1u]);
-        for (int j0 = s & ~3; j0 < e; j0 += 32) {
-            const int left = e - j0;
-            uint32_t acc = 0u;
-            test16(j0, acc);
-            if (left > 16) test16(j0 + 16, acc);
-            else acc <<= 16;
-            uint32_t mask = __brev(acc);
-            // Keep bits of [s, e) only, and drop the particle itself.
-            uint32_t valid = left >= 32 ? 0xffffffffu : ((1u << left) - 1u);
-            if (j0 < s) valid &= ~((1u << (s - j0)) - 1u);
-            const int self = i - j0;
-            if (self >= 0 && self < 32) valid &= ~(1u << self);
-            mask &= valid;
-            if constexpr (STORE) {
-                while (mask) {
-                    const int b = __ffs(mask) - 1;
-                    mask &= mask - 1u;
-                    if (count < cap)
-                        out[static_cast<size_t>(count) * stride] =
-                            static_cast<uint32_t>(j0 + b);
-                    ++count;
+    // Rows z -> y, each one index range walked in ascending order -- exactly
+    // the reference's z -> y -> x cell walk (neighbors.cu:52-86).  Each range
+    // is tested in 32-candidate chunks from a multiple of 4 (the second half
+    // of a chunk only if the range reaches it); candidates outside [s, e) and
+    // the particle itself are masked off, and the hits are then appended in
+    // ascending order.  The component arrays are padded (soa_stride_for), so
+    // a chunk may read past the last particle.
+    for (int z = rows.z0; z <= rows.z1; ++z)
+        for (int y = rows.y0; y <= rows.y1; ++y) {
+            int s, e;
+            if (!rows.range(first, z, y, s, e)) continue;
+            for (int j0 = s & ~3; j0 < e; j0 += 32) {
+                uint32_t acc = 0u;
+                test16(j0, acc);
+                if (e - j0 > 16) test16(j0 + 16, acc);
+                else acc <<= 16;
+                uint32_t mask = __brev(acc) & chunk_valid(j0, s, e, i);
+                if constexpr (STORE) {
+                    while (mask) {
+                        const int b = __ffs(mask) - 1;
+                        mask &= mask - 1u;
+                        if (count < cap)
+                            out[static_cast<size_t>(count) * stride] =
+                                static_cast<uint32_t>(j0 + b);
+                        ++count;
+                    }
+                } else {
+                    count += __popc(mask);
                 }
-            } else {
-                count += __popc(mask);
             }
         }
-    };
-    for (int z = z0; z <= z1; ++z)
-        for (int y = y0; y <= y1; ++y) row_walk(z, y);
     return count;
 }
 
@@ -468,7 +485,7 @@ __device__ __forceinline__ void search_tail(const StepConst& c, int i, float4 pi
 }
 
 template <bool LAMBDA, bool B>
-__global__ void PBF_WALK_BOUNDS
+__global__ void __launch_bounds__(kMaxTunedBlock)
 k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
          const float* __restrict__ sy, const float* __restrict__ sz, const int* __restrict__ first,
          StepConst c, int n, uint32_t* __restrict__ nbr, int* __restrict__ cnt,
@@ -480,58 +497,6 @@ k_search(const float4* __restrict__ xs, const float* __restrict__ sx,
     const int count = walk<B>(c, i, pi, sx, sy, sz, first, out, c.max_nb);
     search_tail<LAMBDA, B>(c, i, pi, xs, out, count, cnt, lam, status);
 }
-
-// The stencil rows of particle i, as the walk visits them: range(z, y)
-// gives row (z, y)'s candidate index range [s, e), false where cell
-// pruning leaves the row out (the same decisions as walk()).
-template <bool B>
-struct StencilRows {
-    GridConst g;
-    uint32_t base, gx, gxy;
-    int cx, cy, cz, x0, x1, y0, y1, z0, z1;
-    bool prune;
-    float xb2, xa2, yb2, ya2, zb2, za2, lim2;
-    __device__ __forceinline__ StencilRows(const StepConst& c, int i, float4 pi) {
-        grid_of<B>(c, i, g, base);
-        cell_of(g, pi.x, pi.y, pi.z, cx, cy, cz);
-        const int R = g.radius;
-        x0 = max(0, cx - R);
-        x1 = min(g.gx - 1, cx + R);
-        y0 = max(0, cy - R);
-        y1 = min(g.gy - 1, cy + R);
-        z0 = max(0, cz - R);
-        z1 = min(g.gz - 1, cz + R);
-        gx = static_cast<uint32_t>(g.gx);
-        gxy = gx * static_cast<uint32_t>(g.gy);
-        prune = c.prune_cells && R == 1;
-        xb2 = xa2 = yb2 = ya2 = zb2 = za2 = lim2 = 0.0f;
-        if (prune) {
-            const float eps = 6.103515625e-05f *
-                              (fabsf(pi.x) + fabsf(pi.y) + fabsf(pi.z) + fabsf(g.minx) +
-                               fabsf(g.miny) + fabsf(g.minz) + g.cell);
-            slab_dist2(pi.x, g.minx, g.cell, cx, eps, xb2, xa2);
-            slab_dist2(pi.y, g.miny, g.cell, cy, eps, yb2, ya2);
-            slab_dist2(pi.z, g.minz, g.cell, cz, eps, zb2, za2);
-            lim2 = c.k.h2 * 1.0009765625f;
-        }
-    }
-    __device__ __forceinline__ bool range(const int* __restrict__ first, int z, int y, int& s,
-                                          int& e) const {
-        int xa = x0, xb = x1;
-        if (prune) {
-            const float dyz = (z < cz ? zb2 : (z > cz ? za2 : 0.0f)) +
-                              (y < cy ? yb2 : (y > cy ? ya2 : 0.0f));
-            if (dyz > lim2) return false;
-            if (xa < cx && dyz + xb2 > lim2) xa = cx;
-            if (xb > cx && dyz + xa2 > lim2) xb = cx;
-        }
-        const uint32_t row =
-            base + static_cast<uint32_t>(y) * gx + static_cast<uint32_t>(z) * gxy;
-        s = __ldg(&first[row + static_cast<uint32_t>(xa)]);
-        e = __ldg(&first[row + static_cast<uint32_t>(xb) + 1u]);
-        return true;
-    }
-};
 
 // The walk on a group of L lanes (gmask; lane `sub`), for scenes too small
 // to fill the GPU with one thread per particle.  The lanes visit the same
@@ -561,7 +526,6 @@ __device__ __forceinline__ int walk_chunks(const StepConst& c, int i, int sub, u
             int s, e;
             if (!rows.range(first, z, y, s, e)) continue;
             for (int j0 = s & ~3; j0 < e; j0 += 32) {
-                const int left = e - j0;
                 const int jb = j0 + sub * W;
                 uint32_t acc = 0u;
                 if (jb < e) {
@@ -589,11 +553,7 @@ __device__ __forceinline__ int walk_chunks(const StepConst& c, int i, int sub, u
                 uint32_t mask = (W == 32 ? __brev(acc) : (__brev(acc) >> (32 - W))) << (sub * W);
 #pragma unroll
                 for (int d = 1; d < L; d <<= 1) mask |= __shfl_xor_sync(gmask, mask, d, L);
-                uint32_t valid = left >= 32 ? 0xffffffffu : ((1u << left) - 1u);
-                if (j0 < s) valid &= ~((1u << (s - j0)) - 1u);
-                const int self = i - j0;
-                if (self >= 0 && self < 32) valid &= ~(1u << self);
-                mask &= valid;
+                mask &= chunk_valid(j0, s, e, i);
                 uint32_t mine = mask & own;
                 int pos = count + __popc(mask & lower);
                 while (mine) {
@@ -677,7 +637,7 @@ __device__ __forceinline__ float lambda_group(const StepConst& c, int i, int sub
 // particle, where a walk is bound by the latency of one thread's row after
 // row.
 template <bool LAMBDA, bool B, int L>
-__global__ void PBF_WALK_BOUNDS
+__global__ void __launch_bounds__(kMaxTunedBlock)
 k_search_split(const float4* __restrict__ xs, const float* __restrict__ sx,
                const float* __restrict__ sy, const float* __restrict__ sz,
                const int* __restrict__ first, StepConst c, int n, uint32_t* __restrict__ nbr,
@@ -704,7 +664,7 @@ k_search_split(const float4* __restrict__ xs, const float* __restrict__ sx,
 
 // Compact lists, first pass: the walk's neighbour count only.
 template <bool B>
-__global__ void PBF_WALK_BOUNDS
+__global__ void __launch_bounds__(kMaxTunedBlock)
 k_count(const float4* __restrict__ xs, const float* __restrict__ sx,
         const float* __restrict__ sy, const float* __restrict__ sz,
         const int* __restrict__ first, StepConst c, int n, int* __restrict__ cnt,
@@ -1129,7 +1089,7 @@ __device__ __forceinline__ void xsph_tail(const StepConst& c, int i, float4 pi,
 // updated ones, computed before this walk), with the velocity response when
 // no vorticity pass follows.
 template <bool B>
-__global__ void PBF_WALK_BOUNDS
+__global__ void __launch_bounds__(kMaxTunedBlock)
 k_search_xsph(const float4* __restrict__ xs, const float* __restrict__ sx,
               const float* __restrict__ sy, const float* __restrict__ sz,
               const int* __restrict__ first, StepConst c, int n, uint32_t* __restrict__ nbr,
@@ -1145,7 +1105,7 @@ k_search_xsph(const float4* __restrict__ xs, const float* __restrict__ sx,
 // k_search_xsph with L lanes per particle: the group walks together
 // (walk_chunks) and shares the XSPH terms; lane 0 writes.
 template <bool B, int L>
-__global__ void PBF_WALK_BOUNDS
+__global__ void __launch_bounds__(kMaxTunedBlock)
 k_search_xsph_split(const float4* __restrict__ xs, const float* __restrict__ sx,
                     const float* __restrict__ sy, const float* __restrict__ sz,
                     const int* __restrict__ first, StepConst c, int n,
