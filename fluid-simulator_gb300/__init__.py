@@ -403,7 +403,7 @@ class PBFSolver:
         return k.value
 
     def set_walk_lanes(self, lanes: int):
-        """pbf_set_walk_lanes: 1, 2 or 4 lanes per particle, 0 = default."""
+        """pbf_set_walk_lanes: 1, 2, 4 or 8 lanes per particle, 0 = default."""
         self._check(self._L.pbf_set_walk_lanes(self._h, int(lanes)))
 
     def set_particles(self, positions, velocities, count: Optional[int] = None):

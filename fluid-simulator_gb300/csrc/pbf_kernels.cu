@@ -1478,24 +1478,29 @@ void launch_gather_first(const uint32_t* perm, const float4* xs_in, float4* xs_o
 }
 inline int tuned_block(const StepConst& c, int k) { return c.blk[k] > 0 ? c.blk[k] : kBlock; }
 
-// Scene size below which a group of 4 lanes walks each particle by default.
-// Measured steps of the dam break at 1 / 2 / 4 lanes: 0.280 / 0.329 / 0.248 ms
-// at 16,384 particles, 0.257 / 0.343 / 0.286 at 32,768, 0.316 / 0.399 / 0.424 at
-// 65,536 (from there on the GPU is full with one lane per particle).
+// Scene sizes for which a group of 8 or 4 lanes walks each particle by
+// default.  Measured steps of dam breaks at 1 / 4 / 8 lanes: 0.219 / 0.206 /
+// 0.174 ms at 8,192 particles, 0.270 / 0.230 / 0.215 at 16,384, 0.249 / 0.242
+// / 0.237 at 20,480, 0.262 / 0.247 / 0.268 at 24,576, 0.269 / 0.255 / 0.291 at
+// 28,672 and 0.274 / 0.283 / 0.334 at 32,768; 2 lanes are slower than 1 or 4
+// (0.329 ms at 16,384, 0.399 at 65,536 against 0.316 for 1 lane: from there
+// on the GPU is full with one lane per particle).
+constexpr size_t kSplitWalk8Max = 20480;
 constexpr size_t kSplitWalk4Below = size_t(1) << 15;
 
 // Lanes per particle of a launch: c.walk_lanes where the split walk applies.
 inline int split_lanes(const StepConst& c, int n) {
     const int L = c.walk_lanes;
-    if ((L != 2 && L != 4) || c.nb_off != nullptr || c.max_nb < L ||
+    if ((L != 2 && L != 4 && L != 8) || c.nb_off != nullptr || c.max_nb < L ||
         static_cast<long long>(n) * L > (1LL << 30))
         return 1;
     return L;
 }
 
 int default_walk_lanes(size_t n, int max_nb) {
-    const int L = n < kSplitWalk4Below ? 4 : 1;
-    return max_nb >= L ? L : 1;
+    int L = n <= kSplitWalk8Max ? 8 : (n < kSplitWalk4Below ? 4 : 1);
+    while (L > 1 && max_nb < L) L /= 2;  // a group never has more lanes than list slots
+    return L;
 }
 
 template <bool LAMBDA, bool B>
@@ -1503,7 +1508,10 @@ void launch_search_split(int L, int bs, const float4* xs, const float* sx, const
                          const float* sz, const int* first, const StepConst& c, int n,
                          uint32_t* nbr, int* cnt, float* lam, unsigned* status, cudaStream_t st) {
     const unsigned g = blocks_for(static_cast<size_t>(n) * L, bs);
-    if (L == 4)
+    if (L == 8)
+        launch_k(k_search_split<LAMBDA, B, 8>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr, cnt,
+                 lam, status);
+    else if (L == 4)
         launch_k(k_search_split<LAMBDA, B, 4>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr, cnt,
                  lam, status);
     else
@@ -1545,6 +1553,23 @@ void launch_search(const float4* xs, const float* sx, const float* sy, const flo
                  status);
 }
 
+template <bool B>
+void launch_search_xsph_split(int L, unsigned g, int bs, const float4* xs, const float* sx,
+                              const float* sy, const float* sz, const int* first,
+                              const StepConst& c, int n, uint32_t* nbr, int* cnt, const float4* v,
+                              float4* v_out, const float4* vin, bool resolve, unsigned* status,
+                              cudaStream_t st) {
+    if (L == 8)
+        launch_k(k_search_xsph_split<B, 8>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr, cnt, v,
+                 v_out, vin, resolve, status);
+    else if (L == 4)
+        launch_k(k_search_xsph_split<B, 4>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr, cnt, v,
+                 v_out, vin, resolve, status);
+    else
+        launch_k(k_search_xsph_split<B, 2>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr, cnt, v,
+                 v_out, vin, resolve, status);
+}
+
 void launch_search_xsph(const float4* xs, const float* sx, const float* sy, const float* sz,
                         const int* first, const StepConst& c, int n, uint32_t* nbr, int* cnt,
                         const float4* v, float4* v_out, const float4* vin, bool resolve,
@@ -1552,18 +1577,12 @@ void launch_search_xsph(const float4* xs, const float* sx, const float* sy, cons
     const int bs = tuned_block(c, kTunedSearch);
     if (const int L = split_lanes(c, n); L > 1) {
         const unsigned g = blocks_for(static_cast<size_t>(n) * L, bs);
-        if (c.scenes && L == 4)
-            launch_k(k_search_xsph_split<true, 4>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr,
-                     cnt, v, v_out, vin, resolve, status);
-        else if (c.scenes)
-            launch_k(k_search_xsph_split<true, 2>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr,
-                     cnt, v, v_out, vin, resolve, status);
-        else if (L == 4)
-            launch_k(k_search_xsph_split<false, 4>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr,
-                     cnt, v, v_out, vin, resolve, status);
+        if (c.scenes)
+            launch_search_xsph_split<true>(L, g, bs, xs, sx, sy, sz, first, c, n, nbr, cnt, v,
+                                           v_out, vin, resolve, status, st);
         else
-            launch_k(k_search_xsph_split<false, 2>, g, bs, st, xs, sx, sy, sz, first, c, n, nbr,
-                     cnt, v, v_out, vin, resolve, status);
+            launch_search_xsph_split<false>(L, g, bs, xs, sx, sy, sz, first, c, n, nbr, cnt, v,
+                                            v_out, vin, resolve, status, st);
         return;
     }
     const unsigned g = blocks_for(n, bs);
@@ -1611,7 +1630,10 @@ void launch_delta_apply_b(const float4* xs, const uint32_t* nbr, const int* cnt,
     const int L = split_lanes(c, n);
     const unsigned gl = blocks_for(static_cast<size_t>(n) * L, bs);
 #define PBF_DELTA_CASE(N)                                                                        \
-    if (L == 4)                                                                                  \
+    if (L == 8)                                                                                  \
+        launch_k(k_delta_apply<N, B, 8>, gl, bs, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out,  \
+                 moved, pre, status);                                                            \
+    else if (L == 4)                                                                             \
         launch_k(k_delta_apply<N, B, 4>, gl, bs, st, xs, nbr, cnt, lam, c, n, xs_out, keys_out,  \
                  moved, pre, status);                                                            \
     else if (L == 2)                                                                             \
@@ -1663,7 +1685,10 @@ void launch_vorticity(const float4* x, const float4* v, const uint32_t* nbr, con
     const int bs = tuned_block(c, kTunedVorticity);
     const int L = split_lanes(c, n);
     const unsigned gl = blocks_for(static_cast<size_t>(n) * L, bs);
-    if (L == 4)
+    if (L == 8)
+        launch_k(k_vorticity_group<8>, gl, bs, st, x, v, nbr, cnt, c, n, omega, store_norm,
+                 status);
+    else if (L == 4)
         launch_k(k_vorticity_group<4>, gl, bs, st, x, v, nbr, cnt, c, n, omega, store_norm,
                  status);
     else if (L == 2)

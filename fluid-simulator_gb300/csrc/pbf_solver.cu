@@ -1173,8 +1173,8 @@ pbf_status pbf_sort_tile(const pbf_solver* s, int* keys_per_tile) {
 
 pbf_status pbf_set_walk_lanes(pbf_solver* s, int lanes) {
     PBF_GUARD(s, {
-        if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4)
-            fail(PBF_ERR_INVALID_ARGUMENT, "walk lanes must be 0, 1, 2 or 4");
+        if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8)
+            fail(PBF_ERR_INVALID_ARGUMENT, "walk lanes must be 0, 1, 2, 4 or 8");
         s->tuned_lanes = lanes;
         s->clear_graphs();
     });

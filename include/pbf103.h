@@ -170,11 +170,11 @@ pbf_status pbf_block_sizes(const pbf_solver* s, int* sizes, int count);
  * else 1,024 below 2^19 particles and 4,096 from there on). */
 pbf_status pbf_sort_tile(const pbf_solver* s, int* keys_per_tile);
 /* Lanes per particle of the list-writing walks in use: the value set by
- * pbf_set_walk_lanes, else 4 below 32,768 particles and 1 from there on (always 1 with
- * compact lists; at most max_neighbors). */
+ * pbf_set_walk_lanes, else 8 up to 20,480 particles, 4 below 32,768 and 1 from
+ * there on (always 1 with compact lists; at most max_neighbors). */
 pbf_status pbf_walk_lanes(const pbf_solver* s, int* lanes);
-/* Sets the lanes per particle of the walks: 1, 2 or 4, or 0 for the default
- * by scene size.  Results do not change.  A lane group pays when one small
+/* Sets the lanes per particle of the walks: 1, 2, 4 or 8, or 0 for the
+ * default by scene size.  Results do not change.  A lane group pays when one small
  * scene leaves the GPU idle; many small solvers running at once on separate
  * streams fill it already and step faster with 1. */
 pbf_status pbf_set_walk_lanes(pbf_solver* s, int lanes);

@@ -70,12 +70,12 @@ def test_use_before_initialize(pbf):
 
 
 def test_walk_lanes_setting(pbf):
-    """Lanes per particle of the walks: 0 (default), 1, 2 or 4; anything else
-    is rejected and leaves the setting unchanged."""
+    """Lanes per particle of the walks: 0 (default), 1, 2, 4 or 8; anything
+    else is rejected and leaves the setting unchanged."""
     s = pbf.PBFSolver()
     s.set_walk_lanes(2)
     assert s.walk_lanes() == 2
-    for bad in (-1, 3, 8):
+    for bad in (-1, 3, 16):
         with pytest.raises(pbf.InvalidArgument):
             s.set_walk_lanes(bad)
     assert s.walk_lanes() == 2

@@ -23,11 +23,11 @@ def run_alone(pbf, per, steps):
     return out
 
 
-@pytest.mark.parametrize("steps,lanes", [(1, 0), (6, 1), (6, 4)])
+@pytest.mark.parametrize("steps,lanes", [(1, 0), (6, 1), (6, 4), (6, 8)])
 def test_batch_equals_each_scene_alone(pbf, scenes, steps, lanes):
     """Every scene of a batch steps bit for bit as it does alone (each scene
-    alone walks split over 4 lanes, the default below 32,768 particles; the
-    batch of 28,716 particles with the default, 1 or 4 lanes)."""
+    alone walks split over 8 lanes, the default up to 20,480 particles; the
+    batch of 28,716 particles with the default, 1, 4 or 8 lanes)."""
     sc, prm, pos, vel, per = scenes.batched_scenes(n_scenes=12, n_min=512, n_max=8192, seed=11)
     b = pbf.PBFSolver()
     b.initialize_batch(sc, prm)
@@ -113,11 +113,11 @@ def test_autotune_keeps_results_and_state(pbf, scenes):
     a.set_particles(pos, vel)
     a.run(3)
     x0, v0 = a.copy_positions_to_host(), a.copy_velocities_to_host()
-    assert a.walk_lanes() == 4  # default below 32,768 particles
+    assert a.walk_lanes() == 8  # default up to 20,480 particles
     sizes = a.autotune(1)
     assert sizes.pop("sort_tile") in (1024, 4096)
     assert set(sizes.values()) <= {64, 128, 256, 512}
-    assert a.walk_lanes() == 4  # the tuner leaves the lanes alone
+    assert a.walk_lanes() == 8  # the tuner leaves the lanes alone
     np.testing.assert_array_equal(a.copy_positions_to_host(), x0)
     np.testing.assert_array_equal(a.copy_velocities_to_host(), v0)
     a.run(4)
@@ -129,10 +129,10 @@ def test_autotune_keeps_results_and_state(pbf, scenes):
     np.testing.assert_array_equal(a.copy_velocities_to_host(), b.copy_velocities_to_host())
 
 
-@pytest.mark.parametrize("lanes", [1, 2, 4])
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8])
 def test_walk_lanes_change_no_result(pbf, scenes, orc, lanes):
-    """Splitting each particle's stencil rows over 1, 2 or 4 lanes writes the
-    same lists: steps stay bit for bit those of the FP32 oracle."""
+    """Splitting each particle's stencil rows over 1, 2, 4 or 8 lanes writes
+    the same lists: steps stay bit for bit those of the FP32 oracle."""
     pos, vel, mn, mx, prm, _ = scenes.dam_break_16k()
     s = pbf.PBFSolver()
     s.initialize(len(pos), mn, mx, prm)

@@ -203,11 +203,12 @@ def test_neighbor_lists_bit_exact_vs_oracle_slot_order(pbf, scenes, orc):
         assert_bitwise(nb[k * n:(k + 1) * n][used], onb[k * n:(k + 1) * n][used], "slot %d" % k)
 
 
-def test_group_walk_line_of_particles(pbf, scenes, orc):
-    """Small scenes walk each particle's stencil on a group of four lanes,
-    each lane testing its quarter of every 32-candidate chunk and writing its
-    own hits in list order.  A line of particles along x puts every
-    neighbour in one row, so one chunk holds hits of several lanes; the
+@pytest.mark.parametrize("lanes", [4, 8])
+def test_group_walk_line_of_particles(pbf, scenes, orc, lanes):
+    """Small scenes walk each particle's stencil on a group of four or eight
+    lanes, each lane testing its share of every 32-candidate chunk and
+    writing its own hits in list order.  A line of particles along x puts
+    every neighbour in one row, so one chunk holds hits of several lanes; the
     lists, counts and the whole step are the one-lane result, bit for bit."""
     k = 200
     pos = np.ones((k, 4), np.float32)
@@ -218,12 +219,13 @@ def test_group_walk_line_of_particles(pbf, scenes, orc):
     prm = scenes.dam_break_params()
     s, o = make_pair(pbf, orc, (pos, vel, (0.0, 0.0, 0.0), (4.2, 1.0, 1.0), prm, {}),
                      max_neighbors=32)
+    s.set_walk_lanes(lanes)
     s.run(3)
     assert o.run(3) == 0
     assert_bitwise(s.copy_positions_to_host(), o.positions(), "positions")
     assert_bitwise(s.copy_velocities_to_host(), o.velocities(), "velocities")
     wp, wid, wcnt = s.working_state()
     op, oid, ocnt = o.working()
-    assert s.walk_lanes() == 4
-    assert wcnt.max() > 8, "hits must span several lanes' quarters of a chunk"
+    assert s.walk_lanes() == lanes
+    assert wcnt.max() > 8, "hits must span several lanes' shares of a chunk"
     assert_bitwise(wcnt, ocnt, "neighbour counts")
