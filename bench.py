@@ -516,8 +516,8 @@ def batched(pkg, scenes, steps: int, warmup: int, per_scene_steps: int):
         return time.perf_counter() - t0
 
     # Each baseline takes its better walk setting: the size rule (scenes below
-    # 32,768 particles split their walks over 4 lanes, best for one scene at a
-    # time) or 1 lane per particle (best when many solvers share the GPU).
+    # 32,768 particles split their walks over 8 or 4 lanes, best for one scene
+    # at a time) or 1 lane per particle (best when many solvers share the GPU).
     timed = {}
     for lanes in (0, 1):
         for a in solvers:
